@@ -1,0 +1,210 @@
+/*
+ * gpw.h -- C ABI of libgpw_gb300: collocate / integrate of Gaussian-pair
+ * densities on periodic real-space grids, on one NVIDIA GB300 (sm_103a).
+ *
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (GPW_SUCCESS == 0) and never aborts or traps.  A failed call leaves a
+ * message for gpw_last_error_string().  Device pointers are owned by the
+ * caller; plans and task sets own their workspaces.
+ *
+ * Reference interfaces replaced (mtaillefumier/libgpw):
+ *   grid_collocate_pgf_product_rspace   src/lib/grid_base_ref_c.h:40-67
+ *                                       src/lib/grid_base_ref_c.cc:1018-1185
+ *   collocate_core<T> / integrate_core<T> src/lib/collocate.cc:543-623, :438-541
+ *   integrate<T> (grid -> matrix elements) src/lib/collocate.cc:626-679
+ */
+#ifndef GPW_H
+#define GPW_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPW_MAX_LEVELS 8
+#define GPW_MAX_L 4          /* largest la_max / lb_max of one primitive    */
+#define GPW_MAX_LP 10        /* la_max + lb_max (+2 for tau)                 */
+
+enum gpw_status {
+    GPW_SUCCESS = 0,
+    GPW_ERR_INVALID_ARG = 1,   /* bad argument, caught on the host           */
+    GPW_ERR_CUDA = 2,          /* CUDA runtime error                          */
+    GPW_ERR_OUT_OF_WINDOW = 3, /* a non-periodic cube leaves the local grid   */
+    GPW_ERR_UNSUPPORTED = 4,   /* valid input that this build does not handle */
+    GPW_ERR_NO_DEVICE = 5,
+    GPW_ERR_ALLOC = 6,
+    GPW_ERR_TIMEOUT = 7        /* a bounded device wait gave up               */
+};
+
+/* Arithmetic of the cube contraction. */
+enum gpw_precision {
+    GPW_PREC_FP64 = 0,   /* plain FP64 kernels, one CTA per pair, FP64 atomics   */
+    GPW_PREC_MIXED = 1   /* tiled kernels: FP64 pair set-up, split-FP32 tables,   */
+                         /* tensor-core cube contraction, compensated            */
+                         /* accumulation, one FP64 write per grid point          */
+};
+
+/*
+ * One grid level.  Mirrors the geometry arguments of
+ * grid_collocate_pgf_product_rspace (grid_base_ref_c.h:20-27,49-56).
+ * The grid array of a level is double[ngrid[2]][ngrid[1]][ngrid[0]] (x fastest),
+ * as the reference's mdarray<double,3,CblasRowMajor> grid(k,j,i).
+ * dh[i] is the step vector of grid axis i (Cartesian), dh_inv its inverse,
+ * used transposed as in grid_base_ref_c.cc:539.
+ */
+typedef struct gpw_grid_desc {
+    int npts[3];
+    int ngrid[3];
+    int lb_grid[3];
+    int periodic[3];
+    double dh[3][3];
+    double dh_inv[3][3];
+    int ortho;       /* 1: orthorhombic algorithm (use_ortho), 0: general cell */
+    int pad_;
+} gpw_grid_desc;
+
+/*
+ * One primitive pair (task).  Mirrors the per-call scalar arguments of
+ * grid_collocate_pgf_product_rspace (grid_base_ref_c.h:40-66).
+ * The density block element P(jco, ico) is pab[pab_offset + (o2+jco)*maxco + (o1+ico)]
+ * with ico/jco the Cartesian (coset) indices of a and b, as pab(o2+jco, o1+ico)
+ * in grid_base_ref_c.cc:185.  Integrate writes matrix elements to the same
+ * place of its hab buffer.
+ * Cube shape: sphere_offset < 0 takes the cube from `radius` by the library's
+ * sphere rule (gpw_sphere_bounds); otherwise the cube is the CP2K-format
+ * run-length list at sphere_table[sphere_offset...] with lb_cube/ub_cube
+ * (grid_base_ref_c.cc:413-471).
+ */
+typedef struct gpw_task {
+    double zeta, zetb, rscale;
+    double ra[3];
+    double rab[3];
+    double radius;
+    int64_t pab_offset;
+    int64_t sphere_offset;
+    int la_max, la_min, lb_max, lb_min;
+    int level;
+    int maxco;
+    int o1, o2;
+    int lb_cube[3];
+    int ub_cube[3];
+} gpw_task;
+
+typedef struct gpw_plan gpw_plan;       /* grid levels bound to one device   */
+typedef struct gpw_taskset gpw_taskset; /* uploaded, sorted and binned pairs */
+
+/* Last error message of the calling thread ("" if none). */
+const char *gpw_last_error_string(void);
+
+/* Library version string. */
+const char *gpw_version(void);
+
+/*
+ * The library's cube rule.  For a sphere of `radius` on an orthorhombic grid
+ * with steps dh[0][0], dh[1][1], dh[2][2], writes lb_cube/ub_cube and the
+ * CP2K-format run-length list (kgmin, then per kg: jgmin, then per jg: igmin)
+ * that grid_collocate_core consumes (grid_base_ref_c.cc:413-471).  Returns the
+ * list length, or -needed if cap is too small, or 0 on a bad argument.
+ * Pure host function.
+ */
+int gpw_sphere_bounds(double radius, const double dh[3][3], int lb_cube[3],
+                      int ub_cube[3], int *sphere_bounds, int cap);
+
+/* Plans ---------------------------------------------------------------- */
+int gpw_plan_create(gpw_plan **plan, int nlevels, const gpw_grid_desc *levels,
+                    int device);
+int gpw_plan_destroy(gpw_plan *plan);
+
+/*
+ * Uploads and analyses a task list (host memory) for repeated collocate /
+ * integrate calls: validation, sorting by level and grid tile, per-tile work
+ * lists.  compute_tau selects the kinetic-energy density (grid_base_ref_c.cc:889-900).
+ * sphere_table (host, may be NULL) holds the CP2K-format lists that tasks with
+ * sphere_offset >= 0 index.  Allocates device memory; synchronous.
+ */
+int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks,
+                       int compute_tau, const int *sphere_table,
+                       int64_t sphere_table_len, gpw_taskset **out);
+int gpw_taskset_destroy(gpw_taskset *ts);
+/* Number of elements the pab / hab buffer must hold for this task set. */
+int64_t gpw_taskset_pab_extent(const gpw_taskset *ts);
+
+/*
+ * grid[level] += sum over tasks of the pair density (grid_base_ref_c.cc:1018).
+ * d_pab and d_grids[l] are device pointers; asynchronous on `stream`
+ * (a cudaStream_t, NULL = legacy default); no allocation, so the call can be
+ * captured in a CUDA graph.
+ */
+int gpw_collocate(gpw_taskset *ts, int precision, const double *d_pab,
+                  double *const *d_grids, void *stream);
+
+/*
+ * d_hab += <V | pair basis functions>: the adjoint of gpw_collocate with respect
+ * to the density block (the role of integrate<T>, collocate.cc:626-679).
+ */
+int gpw_integrate(gpw_taskset *ts, int precision, double *const *d_grids,
+                  double *d_hab, void *stream);
+
+/*
+ * Backward pass of E = sum_levels <V_level, rho_level>: with V given per level,
+ * accumulates dE/dpab into d_hab (== gpw_integrate), and per task dE/dRa,
+ * dE/dRb (double[3*ntasks], task order as given) and dE/dzeta, dE/dzetb
+ * (double[ntasks]).  Any of the gradient outputs may be NULL.  Recomputes the
+ * 1-D tables; stores nothing between forward and backward.
+ */
+int gpw_backward(gpw_taskset *ts, const double *d_pab, double *const *d_grids,
+                 double *d_hab, double *d_dra, double *d_drb, double *d_dzeta,
+                 double *d_dzetb, void *stream);
+
+/*
+ * Waits for `stream` and reports device-side error flags raised since the
+ * last check (e.g. GPW_ERR_OUT_OF_WINDOW, GPW_ERR_TIMEOUT).
+ */
+int gpw_taskset_check(gpw_taskset *ts, void *stream);
+
+/* Host-buffer convenience calls (copies inside, synchronous) ------------- */
+int gpw_collocate_host(gpw_taskset *ts, int precision, const double *h_pab,
+                       double *const *h_grids);
+int gpw_integrate_host(gpw_taskset *ts, int precision, double *const *h_grids,
+                       double *h_hab);
+
+/*
+ * Drop-in form of grid_collocate_pgf_product_rspace (grid_base_ref_c.h:40-67)
+ * with mdarray arguments replaced by raw row-major arrays:
+ *   dh, dh_inv   double[3][3]
+ *   pab          double[maxco][maxco]
+ *   grid         double[ngrid[2]][ngrid[1]][ngrid[0]]  (host, accumulated)
+ * Runs the FP64 GPU path on the current device (default 0).  lb_cube, ub_cube
+ * and sphere_bounds are read only when use_ortho != 0, as in the reference.
+ */
+int gpw_collocate_pgf_product_rspace(
+    int compute_tau, int use_ortho, int la_max, int la_min, int lb_max,
+    int lb_min, double zeta, double zetb, double rscale, const double dh[3][3],
+    const double dh_inv[3][3], const double ra[3], const double rab[3],
+    const int npts[3], const int ngrid[3], const int lb_grid[3],
+    const int periodic[3], int lmax, double radius, const int lb_cube[3],
+    const int ub_cube[3], int nspheres, const int *sphere_bounds, int maxco,
+    int o1, int o2, const double *pab, double *grid);
+
+/*
+ * Dense cube contraction of the factorised prototype, on the device:
+ *   collocate_core: out[z][y][x] = sum co[a][g][b] * pol[0][g][z] * pol[1][b][y] * pol[2][a][x]
+ *     (collocate.cc:543-623; naive form collocate_test.cc:11-33)
+ *   integrate_core: co[g][b][a] = sum V[z][y][x] * pol[0][g][z] * pol[1][b][y] * pol[2][a][x]
+ *     (collocate.cc:438-541; naive form collocate_test.cc:77-99)
+ * length = {nz, ny, nx}; pol is double[3][L][ld_pol] with ld_pol >= max(length);
+ * co is double[L][L][L].  All pointers are device pointers; FP64.
+ */
+int gpw_collocate_core(const int length[3], int L, const double *d_co,
+                       const double *d_pol, int ld_pol, double *d_out,
+                       void *stream);
+int gpw_integrate_core(const int length[3], int L, const double *d_pol,
+                       int ld_pol, const double *d_V, double *d_co,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GPW_H */
