@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark: collocate + integrate pairs/s on one GB300.
+
+A step is one collocate (density blocks -> grid) plus one integrate (potential
+grid -> matrix elements) over every pair of the workload, through the C ABI.
+Default workload: 1,000,000 pairs, la,lb in {0..4}, exponents log-uniform in
+[0.05, 200], 30-bohr cubic cell, 256^3 grid (seeded synthetic inputs).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--config 1..5] [--precision mixed|fp64] [--npairs n]
+
+--impl reference times the CPU implementation of the same path on the host
+cores (the oracle port of the reference's FP64 collocate; the reference's own
+library where it was built) on a bounded sample of the same workload.
+Multi-GPU runs are independent replicas (weak scaling, no collective).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "collocate+integrate pairs/s on 1 GB300: batched FP32/3xTF32 vs plain FP64, ≤1e-8 err"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=5)
+    ap.add_argument("--npairs", type=int, default=None)
+    ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline sample budget")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-error", action="store_true", help="skip the FP64 error check of the mixed path")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self) -> dict:
+        rows = []
+        for ln in (self.out or "").splitlines():
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                rows.append((float(p[1]), float(p[2]), p[5], p[6], p[7], p[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sm = sorted(r[0] for r in rows)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[2:]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": rows[0][1], "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+# ----------------------------------------------------------------------------
+def algorithmic_flops(wl) -> tuple:
+    """Collocate flops of the dense three-stage contraction per pair,
+    2L*nx*ny*nz + 2L^2*nz*ny + 2L^3*nz, with n the cube extents of the library's
+    cube rule (box of the general cell); integrate is symmetric.  Also returns
+    the cube points."""
+    from libgpw_gb300 import tasks as T
+
+    t = wl.tasks
+    L = (t["la_max"] + t["lb_max"] + 1 + 2 * wl.compute_tau).astype(np.float64)
+    n = np.zeros((t.shape[0], 3))
+    for lev_i, g in enumerate(wl.levels):
+        m = t["level"] == lev_i
+        if g["ortho"]:
+            for d in range(3):
+                n[m, d] = 2 * np.floor(t["radius"][m] / g["dh"][d][d]) + 2
+        else:
+            inv = np.abs(np.asarray(g["dh_inv"]))
+            span = t["radius"][m][:, None] * inv.sum(axis=0)[None, :]
+            n[m] = 2 * np.ceil(span) + 1
+    nz, ny, nx = n[:, 2], n[:, 1], n[:, 0]
+    fl = 2 * L * nx * ny * nz + 2 * L ** 2 * nz * ny + 2 * L ** 3 * nz
+    return float(fl.sum()), float((nx * ny * nz).sum())
+
+
+def subsample(wl, idx):
+    """A Workload holding the pairs idx with a compact density-block buffer."""
+    from libgpw_gb300 import tasks as T
+
+    t = wl.tasks[idx].copy()
+    nsa = (t["maxco"]).astype(np.int64)
+    nsb = ((t["lb_max"] + 1) * (t["lb_max"] + 2) // 2).astype(np.int64)
+    blk = nsa * nsb
+    off = np.zeros(len(idx), np.int64)
+    off[1:] = np.cumsum(blk[:-1])
+    pab = np.concatenate([wl.pab[int(o): int(o) + int(b)] for o, b in zip(wl.tasks["pab_offset"][idx], blk)])
+    t["pab_offset"] = off
+    return T.Workload(wl.name + "_sample", t, wl.levels, pab, compute_tau=wl.compute_tau)
+
+
+def cpu_baseline(wl, seconds: float, seed: int = 0) -> dict:
+    """The CPU FP64 path (oracle port) on a random pair sample, all host threads."""
+    from oracle import oracle as O
+
+    O.build()
+    kind = "port"
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    V = None
+    n = 16
+    elapsed = 0.0
+    while True:
+        idx = np.sort(rng.choice(wl.ntasks, size=min(n, wl.ntasks), replace=False))
+        sw = subsample(wl, idx)
+        if V is None:
+            V = [np.random.default_rng(1).uniform(-1, 1, size=g.shape) for g in
+                 [np.zeros((int(l["ngrid"][2]), int(l["ngrid"][1]), int(l["ngrid"][0])), dtype=np.int8)
+                  for l in wl.levels]]
+        t0 = time.perf_counter()
+        O.batch(sw, nthreads=threads)
+        O.batch(sw, V=V, nthreads=threads)
+        elapsed = time.perf_counter() - t0
+        if elapsed >= seconds * 0.4 or n >= wl.ntasks:
+            break
+        n = int(min(wl.ntasks, max(2 * n, n * seconds * 0.6 / max(elapsed, 1e-3))))
+    return {"value": len(idx) / elapsed, "unit": "pairs/s", "cores": threads, "kind": kind,
+            "sample": f"{len(idx)} random pairs of the {wl.ntasks}-pair workload, collocate+integrate FP64, "
+                      f"{threads} threads with private grids, {elapsed:.1f} s"}
+
+
+def reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from libgpw_gb300 import tasks as T
+
+    wl = T.config(args.config, npairs=args.npairs)
+    vals = []
+    base = None
+    for k in range(args.warmup + args.steps):
+        b = cpu_baseline(wl, max(2.0, args.cpu_seconds / 2), seed=k)
+        if k >= args.warmup:
+            vals.append(b["value"])
+            base = b
+    value = float(np.median(vals))
+    base["value"] = value
+    line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wl.ntasks / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "impl": "reference", "config": {"workload": wl.name, "npairs": wl.ntasks, "precision": "fp64-cpu"},
+            "cpu_baseline": base, "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
+                                          "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+# ----------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    import torch
+
+    from libgpw_gb300 import capi, tasks as T
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    wl = T.config(args.config, npairs=args.npairs)
+    t0 = time.perf_counter()
+    plan = capi.Plan(wl.levels, device=local)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    plan_s = time.perf_counter() - t0
+    prec = args.precision
+    pab = torch.from_numpy(wl.pab).to(dev)
+    grids = [torch.zeros(T.grid_shape(g), dtype=torch.float64, device=dev) for g in wl.levels]
+    Vh = wl.potentials(seed=1)
+    V = [torch.from_numpy(v).to(dev) for v in Vh]
+    hab = torch.zeros(ts.pab_extent, dtype=torch.float64, device=dev)
+    if prec == "auto":
+        try:
+            ts.collocate(pab, grids, "mixed")
+            prec = "mixed"
+        except capi.GpwError:
+            prec = "fp64"
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+
+    def step():
+        ts.collocate(pab, grids, prec)
+        ts.integrate(V, hab, prec)
+
+    for _ in range(args.warmup):
+        step()
+    ts.check()
+    torch.cuda.synchronize()
+    ts.stats()
+    ts.profile(True)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record()
+            step()
+            ends[k].record()
+        torch.cuda.synchronize()
+    barrier()
+    ts.check()
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    kern_ms, kern_launches, n_kernels = ts.stats()
+    ts.profile(False)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * wl.ntasks / (ms * 1e-3)
+
+    # error of this precision against the plain FP64 path (relative grid L2, max-abs matrix element)
+    err = {}
+    if not args.no_error:
+        g1 = [torch.zeros_like(g) for g in grids]
+        g2 = [torch.zeros_like(g) for g in grids]
+        h1 = torch.zeros_like(hab)
+        h2 = torch.zeros_like(hab)
+        ts.collocate(pab, g1, prec)
+        ts.collocate(pab, g2, "fp64")
+        ts.integrate(V, h1, prec)
+        ts.integrate(V, h2, "fp64")
+        torch.cuda.synchronize()
+        num = sum(float(torch.sum((a - b) ** 2)) for a, b in zip(g1, g2))
+        den = sum(float(torch.sum(b ** 2)) for b in g2)
+        err = {"grid_rel_l2_vs_fp64": (num / den) ** 0.5 if den > 0 else 0.0,
+               "hab_max_abs_vs_fp64": float(torch.max(torch.abs(h1 - h2))),
+               "hab_max_abs_scale": float(torch.max(torch.abs(h2)))}
+        del g1, g2, h1, h2
+
+    # end to end through the host-buffer C ABI calls (pinned host memory, copies inside the timed region)
+    e2e = None
+    if not args.no_e2e:
+        pab_h = torch.from_numpy(wl.pab).pin_memory().numpy()
+        grids_h = [torch.zeros(T.grid_shape(g), dtype=torch.float64).pin_memory().numpy() for g in wl.levels]
+        V_h = [torch.from_numpy(v).pin_memory().numpy() for v in Vh]
+        hab_h = torch.zeros(ts.pab_extent, dtype=torch.float64).pin_memory().numpy()
+        ts.collocate_host(pab_h, grids_h, prec)
+        ts.integrate_host(V_h, hab_h, prec)
+        ne = max(2, min(args.steps, 5))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(ne):
+            ts.collocate_host(pab_h, grids_h, prec)
+            ts.integrate_host(V_h, hab_h, prec)
+        torch.cuda.synchronize()
+        barrier()
+        e2e_s = (time.perf_counter() - t0) / ne
+        gbytes = sum(g.nbytes for g in grids_h)
+        e2e = {"value": world * wl.ntasks / e2e_s, "unit": "pairs/s",
+               "h2d_bytes_per_step": int(pab_h.nbytes + gbytes + sum(v.nbytes for v in V_h) + hab_h.nbytes),
+               "d2h_bytes_per_step": int(gbytes + hab_h.nbytes), "ms_per_step": e2e_s * 1e3}
+
+    if rank != 0:
+        return
+    flops, points = algorithmic_flops(wl)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    # dominant kernel: the cube contraction launches (collocate + integrate)
+    per_launch_flops = 2 * flops / max(kern_launches / args.steps, 1)
+    avg_launch_ms = kern_ms / max(kern_launches, 1)
+    achieved_tf = per_launch_flops / (avg_launch_ms * 1e-3) / 1e12 if avg_launch_ms > 0 else 0.0
+    if prec == "mixed":
+        peak = peaks.get("bf16_tflops_sustained") or 1700.0
+        roof = {"bound": "tensor", "achieved": achieved_tf, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved_tf / peak, "traffic": None,
+                "peak_source": "bf16 sustained, MEASURED_PEAKS.json (of measured)"}
+    else:
+        hbm = peaks.get("hbm_gbs") or 6800.0
+        gbytes_alg = 16.0 * points  # FP64 read+write per cube point (no reuse)
+        per_launch_b = 2 * gbytes_alg / max(kern_launches / args.steps, 1)
+        ach = per_launch_b / (avg_launch_ms * 1e-3) / 1e9 if avg_launch_ms > 0 else 0.0
+        roof = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": None, "peak_source": "hbm_gbs, MEASURED_PEAKS.json (of measured)"}
+    roof["kernel_ms_per_step"] = kern_ms / args.steps
+    roof["kernel_launches_per_step"] = kern_launches / args.steps
+    roof["algorithmic_tflop_per_step"] = 2 * flops / 1e12
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        cpu = cpu_baseline(wl, args.cpu_seconds)
+    lv = wl.levels[0]
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32-split tf32x3 + f64" if prec == "mixed" else "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": wl.name, "npairs": wl.ntasks,
+                   "grids": ["x".join(str(int(v)) for v in l["ngrid"]) for l in wl.levels],
+                   "precision": prec, "compute_tau": wl.compute_tau,
+                   "l2": "grid and potential exceed L2; a 512 MB buffer is written between timed steps",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "plan_seconds": plan_s},
+        "gpu_launches": int(n_kernels / max(args.steps, 1) * args.steps),
+        "roofline": roof, "error": err, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e,
+        "algorithmic_cube_points": points,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

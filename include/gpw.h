@@ -164,6 +164,18 @@ int gpw_backward(gpw_taskset *ts, const double *d_pab, double *const *d_grids,
  */
 int gpw_taskset_check(gpw_taskset *ts, void *stream);
 
+/*
+ * Profiling counters of a task set, for benchmarks.  With enable != 0 the
+ * library brackets each cube-contraction launch with CUDA events on the
+ * launching stream.  gpw_taskset_stats waits for the device, returns the
+ * accumulated device time of those launches (ms) and their number, and the
+ * number of kernels the library launched for this task set, then resets all
+ * three.  Any output pointer may be NULL.
+ */
+int gpw_taskset_profile(gpw_taskset *ts, int enable);
+int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
+                      int64_t *contraction_launches, int64_t *kernel_launches);
+
 /* Host-buffer convenience calls (copies inside, synchronous) ------------- */
 int gpw_collocate_host(gpw_taskset *ts, int precision, const double *h_pab,
                        double *const *h_grids);

@@ -1,0 +1,698 @@
+// C ABI of libgpw_gb300 (include/gpw.h): plans, task sets, dispatch, the
+// drop-in single-pair entry, and the host-side geometry every kernel reads.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "gpw_internal.h"
+
+using namespace gpw;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+    return fail(GPW_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define GPW_CUDA(call)                                      \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+bool finite3(const double *v) { return std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// Dense polynomials in (d0, d1, d2) up to total degree kMaxLp, index [k][j][i].
+constexpr int NP = kNPow;
+constexpr int NQ = NP * NP * NP;
+void poly_mul(const std::vector<double> &a, int da, const std::vector<double> &b, int db,
+              std::vector<double> &out) {
+    std::fill(out.begin(), out.end(), 0.0);
+    for (int ka = 0; ka <= da; ka++)
+        for (int ja = 0; ja <= da - ka; ja++)
+            for (int ia = 0; ia <= da - ka - ja; ia++) {
+                const double va = a[(ka * NP + ja) * NP + ia];
+                if (va == 0.0) continue;
+                for (int kb = 0; kb <= db; kb++)
+                    for (int jb = 0; jb <= db - kb; jb++)
+                        for (int ib = 0; ib <= db - kb - jb; ib++)
+                            out[((ka + kb) * NP + ja + jb) * NP + ia + ib] += va * b[(kb * NP + jb) * NP + ib];
+            }
+}
+
+// Lattice transform of a general cell: T[q][c], q = (k,j,i) and c = (lz,ly,lx),
+// both packed with pidx(kMaxLp, ...).  Column c holds the coefficients of
+// (x-xp)^lx (y-yp)^ly (z-zp)^lz in the lattice offsets d_a, since
+// r - rp = sum_a d_a dh[a][:]  (the multinomial transform of grid_base_ref_c.cc:646-698).
+std::vector<double> lattice_transform(const double dh[3][3]) {
+    const int NT = ncoef(kMaxLp);
+    std::vector<double> T((size_t)NT * NT, 0.0);
+    std::vector<std::vector<double>> U(3 * NP, std::vector<double>(NQ, 0.0));
+    for (int c = 0; c < 3; c++) {
+        U[c * NP][0] = 1.0;
+        std::vector<double> lin(NQ, 0.0);
+        lin[1] = dh[0][c];
+        lin[NP] = dh[1][c];
+        lin[NP * NP] = dh[2][c];
+        for (int n = 1; n <= kMaxLp; n++) poly_mul(U[c * NP + n - 1], n - 1, lin, 1, U[c * NP + n]);
+    }
+    std::vector<double> tmp(NQ), col(NQ);
+    for (int lz = 0; lz <= kMaxLp; lz++)
+        for (int ly = 0; ly <= kMaxLp - lz; ly++) {
+            poly_mul(U[2 * NP + lz], lz, U[1 * NP + ly], ly, tmp);
+            for (int lx = 0; lx <= kMaxLp - lz - ly; lx++) {
+                poly_mul(tmp, lz + ly, U[0 * NP + lx], lx, col);
+                const int ci = pidx(kMaxLp, lz, ly, lx);
+                const int deg = lx + ly + lz;
+                for (int k = 0; k <= deg; k++)
+                    for (int j = 0; j <= deg - k; j++) {
+                        const int i = deg - k - j;
+                        T[(size_t)pidx(kMaxLp, k, j, i) * NT + ci] = col[(k * NP + j) * NP + i];
+                    }
+            }
+        }
+    return T;
+}
+
+// CP2K-format cube list -> random-access table (kgmin, (jgmin,rowstart)*, igmin*).
+// Returns the number of list entries consumed, or -1 if malformed / outside [lb, ub].
+int convert_list(const int *sb, int64_t avail, const int lb[3], const int ub[3], std::vector<int> &out) {
+    int64_t pos = 0;
+    if (avail < 1) return -1;
+    const int kgmin = sb[pos++];
+    if (kgmin > 0 || kgmin < lb[2] || 1 - kgmin > ub[2]) return -1;
+    const int nk = 1 - kgmin;
+    std::vector<int> head(1 + 2 * nk), rows;
+    head[0] = kgmin;
+    for (int k = 0; k < nk; k++) {
+        if (pos >= avail) return -1;
+        const int jg = sb[pos++];
+        if (jg > 0 || jg < lb[1] || 1 - jg > ub[1]) return -1;
+        head[1 + 2 * k] = jg;
+        head[2 + 2 * k] = (int)rows.size();
+        for (int j = jg; j <= 0; j++) {
+            if (pos >= avail) return -1;
+            const int ig = sb[pos++];
+            if (ig > 0 || ig < lb[0] || 1 - ig > ub[0]) return -1;
+            rows.push_back(ig);
+        }
+    }
+    out.insert(out.end(), head.begin(), head.end());
+    out.insert(out.end(), rows.begin(), rows.end());
+    return (int)pos;
+}
+
+// Host geometry of one pair (grid_base_ref_c.cc:878-900, :534-553, :636-726).
+int make_geom(const gpw_task &t, int idx, const Plan &P, int tau, const int *table, int64_t table_len,
+              PairGeom &g, std::vector<int> &dev_table) {
+    char buf[256];
+    if (t.level < 0 || t.level >= P.nlevels) {
+        snprintf(buf, sizeof buf, "task %d: level %d out of range", idx, t.level);
+        return fail(GPW_ERR_INVALID_ARG, buf);
+    }
+    if (t.la_min < 0 || t.lb_min < 0 || t.la_min > t.la_max || t.lb_min > t.lb_max ||
+        t.la_max > GPW_MAX_L || t.lb_max > GPW_MAX_L) {
+        snprintf(buf, sizeof buf, "task %d: angular momenta out of range (0 <= l_min <= l_max <= %d)", idx,
+                 GPW_MAX_L);
+        return fail(GPW_ERR_INVALID_ARG, buf);
+    }
+    if (!(t.zeta > 0.0) || !(t.zetb > 0.0) || !std::isfinite(t.zeta) || !std::isfinite(t.zetb) ||
+        !(t.radius > 0.0) || !std::isfinite(t.radius) || !std::isfinite(t.rscale) || !finite3(t.ra) ||
+        !finite3(t.rab) || t.maxco < 1) {
+        snprintf(buf, sizeof buf, "task %d: exponents, radius, positions must be finite (and positive)", idx);
+        return fail(GPW_ERR_INVALID_ARG, buf);
+    }
+    const LevelDev &lv = P.lv[t.level];
+    memset(&g, 0, sizeof g);
+    g.task = idx;
+    g.level = t.level;
+    g.ortho = lv.ortho;
+    g.zeta = t.zeta;
+    g.zetb = t.zetb;
+    g.zetp = t.zeta + t.zetb;
+    const double f = t.zetb / g.zetp;
+    const double rab2 = t.rab[0] * t.rab[0] + t.rab[1] * t.rab[1] + t.rab[2] * t.rab[2];
+    g.prefactor = t.rscale * std::exp(-t.zeta * f * rab2);
+    for (int i = 0; i < 3; i++) {
+        g.ra[i] = t.ra[i];
+        g.rp[i] = t.ra[i] + f * t.rab[i];
+        g.rb[i] = t.ra[i] + t.rab[i];
+    }
+    g.la0_max = t.la_max; g.la0_min = t.la_min; g.lb0_max = t.lb_max; g.lb0_min = t.lb_min;
+    if (tau) {
+        g.la_max = t.la_max + 1; g.la_min = std::max(t.la_min - 1, 0);
+        g.lb_max = t.lb_max + 1; g.lb_min = std::max(t.lb_min - 1, 0);
+    } else {
+        g.la_max = t.la_max; g.la_min = t.la_min; g.lb_max = t.lb_max; g.lb_min = t.lb_min;
+    }
+    g.lp = g.la_max + g.lb_max;
+    g.radius = t.radius;
+    g.maxco = t.maxco; g.o1 = t.o1; g.o2 = t.o2;
+    g.pab_offset = t.pab_offset;
+    g.table_off = -1;
+    if (lv.ortho) {
+        for (int i = 0; i < 3; i++) {
+            double s = 0.0;
+            for (int j = 0; j < 3; j++) s += lv.dh_inv[j][i] * g.rp[j];
+            g.cc[i] = (int)std::floor(s);
+            g.off[i] = g.rp[i] - (double)g.cc[i] * lv.dh[i][i];
+        }
+        if (t.sphere_offset >= 0) {
+            if (!table || t.sphere_offset >= table_len) {
+                snprintf(buf, sizeof buf, "task %d: sphere_offset outside the sphere table", idx);
+                return fail(GPW_ERR_INVALID_ARG, buf);
+            }
+            for (int d = 0; d < 3; d++) { g.lb[d] = t.lb_cube[d]; g.hi[d] = t.ub_cube[d]; }
+            g.table_off = (int64_t)dev_table.size();
+            if (convert_list(table + t.sphere_offset, table_len - t.sphere_offset, g.lb, g.hi, dev_table) < 0) {
+                snprintf(buf, sizeof buf, "task %d: malformed cube list or cube outside lb_cube/ub_cube", idx);
+                return fail(GPW_ERR_INVALID_ARG, buf);
+            }
+            g.kgmin = table[t.sphere_offset];
+        } else {
+            for (int d = 0; d < 3; d++) {
+                g.lb[d] = -rule_kmax(t.radius, lv.dh[d][d]);
+                g.hi[d] = 1 - g.lb[d];
+            }
+            g.kgmin = g.lb[2];
+        }
+        // the reference's window assertion (grid_base_ref_c.cc:343-346)
+        for (int d = 0; d < 3; d++) {
+            if (lv.periodic[d]) continue;
+            const int a = axis_index(0, g.cc[d], g.lb[d], g.lb[d], lv.lb_grid[d], lv.npts[d], lv.ngrid[d]);
+            const int b = axis_index(0, g.cc[d], g.hi[d], g.lb[d], lv.lb_grid[d], lv.npts[d], lv.ngrid[d]);
+            if (a < 0 || b < 0) {
+                snprintf(buf, sizeof buf, "task %d: cube leaves the local grid on non-periodic axis %d", idx, d);
+                return fail(GPW_ERR_OUT_OF_WINDOW, buf);
+            }
+        }
+        g.cost = (int64_t)(g.hi[0] - g.lb[0] + 1) * (g.hi[1] - g.lb[1] + 1) * (g.hi[2] - g.lb[2] + 1);
+    } else {
+        for (int i = 0; i < 3; i++) {
+            g.off[i] = 0.0;
+            for (int j = 0; j < 3; j++) g.off[i] += lv.dh_inv[j][i] * g.rp[j];
+        }
+        int imin[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, imax[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+        for (int a = -1; a <= 1; a++)
+            for (int b = -1; b <= 1; b++)
+                for (int c = -1; c <= 1; c++) {
+                    const double x = g.rp[0] + a * t.radius, y = g.rp[1] + b * t.radius, z = g.rp[2] + c * t.radius;
+                    for (int d = 0; d < 3; d++) {
+                        const double s = lv.dh_inv[0][d] * x + lv.dh_inv[1][d] * y + lv.dh_inv[2][d] * z;
+                        imin[d] = std::min(imin[d], (int)std::floor(s));
+                        imax[d] = std::max(imax[d], (int)std::ceil(s));
+                    }
+                }
+        for (int d = 0; d < 3; d++) {
+            g.cc[d] = imin[d];
+            g.hi[d] = imax[d];
+            if (!lv.periodic[d] && imax[d] - imin[d] + imod(imin[d] + lv.lb_grid[d], lv.npts[d]) >= lv.ngrid[d]) {
+                snprintf(buf, sizeof buf, "task %d: box leaves the local grid on non-periodic axis %d", idx, d);
+                return fail(GPW_ERR_OUT_OF_WINDOW, buf);
+            }
+        }
+        g.cost = (int64_t)(imax[0] - imin[0] + 1) * (imax[1] - imin[1] + 1) * (imax[2] - imin[2] + 1);
+    }
+    return GPW_SUCCESS;
+}
+
+GridPtrs grid_ptrs(const Plan &P, double *const *p) {
+    GridPtrs g;
+    memset(&g, 0, sizeof g);
+    for (int l = 0; l < P.nlevels; l++) g.p[l] = p[l];
+    return g;
+}
+
+struct HostStage {
+    double *d_pab = nullptr;
+    double *d_grids[GPW_MAX_LEVELS] = {nullptr};
+    int64_t pab_len = 0;
+};
+std::mutex g_stage_mu;
+std::map<const gpw_taskset *, HostStage> g_stage;
+
+}  // namespace
+
+struct gpw_plan : Plan {};
+struct gpw_taskset : TaskSet {};
+
+extern "C" {
+
+const char *gpw_last_error_string(void) { return g_err.c_str(); }
+
+const char *gpw_version(void) { return "libgpw_gb300 0.1 (sm_103a)"; }
+
+int gpw_sphere_bounds(double radius, const double dh[3][3], int lb_cube[3], int ub_cube[3],
+                      int *sphere_bounds, int cap) {
+    if (!dh || !lb_cube || !ub_cube || !(radius > 0.0) || !std::isfinite(radius) ||
+        !(dh[0][0] > 0.0) || !(dh[1][1] > 0.0) || !(dh[2][2] > 0.0)) {
+        fail(GPW_ERR_INVALID_ARG, "gpw_sphere_bounds: radius and diagonal steps must be positive");
+        return 0;
+    }
+    const double r2 = rmul(radius, radius);
+    const int kmax = rule_kmax(radius, dh[2][2]);
+    int n = 0;
+    auto push = [&](int v) {
+        if (n < cap && sphere_bounds) sphere_bounds[n] = v;
+        n++;
+    };
+    push(-kmax);
+    for (int kg = -kmax; kg <= 0; kg++) {
+        const double remk = rule_remk(r2, kg, dh[2][2]);
+        const int jmax = rule_jmax(remk, dh[1][1]);
+        push(-jmax);
+        for (int jg = -jmax; jg <= 0; jg++) push(-rule_imax(remk, jg, dh[1][1], dh[0][0]));
+    }
+    for (int d = 0; d < 3; d++) {
+        lb_cube[d] = -rule_kmax(radius, dh[d][d]);
+        ub_cube[d] = 1 - lb_cube[d];
+    }
+    return n <= cap ? n : -n;
+}
+
+int gpw_plan_create(gpw_plan **plan, int nlevels, const gpw_grid_desc *levels, int device) {
+    if (!plan || !levels || nlevels < 1 || nlevels > GPW_MAX_LEVELS)
+        return fail(GPW_ERR_INVALID_ARG, "gpw_plan_create: 1..GPW_MAX_LEVELS levels required");
+    *plan = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
+        return fail(GPW_ERR_NO_DEVICE, "gpw_plan_create: no CUDA device");
+    if (device < 0 || device >= ndev) return fail(GPW_ERR_INVALID_ARG, "gpw_plan_create: bad device");
+    gpw_plan *P = new gpw_plan();
+    P->device = device;
+    P->nlevels = nlevels;
+    std::vector<double> tm;
+    for (int l = 0; l < nlevels; l++) {
+        const gpw_grid_desc &d = levels[l];
+        LevelDev &v = P->lv[l];
+        memset(&v, 0, sizeof v);
+        for (int i = 0; i < 3; i++) {
+            v.npts[i] = d.npts[i];
+            v.ngrid[i] = d.ngrid[i];
+            v.lb_grid[i] = d.lb_grid[i];
+            v.periodic[i] = d.periodic[i] ? 1 : 0;
+            if (d.npts[i] < 1 || d.ngrid[i] < 1 || (v.periodic[i] && d.ngrid[i] != d.npts[i])) {
+                delete P;
+                return fail(GPW_ERR_INVALID_ARG,
+                            "gpw_plan_create: npts, ngrid >= 1 and ngrid == npts on periodic axes");
+            }
+            for (int j = 0; j < 3; j++) {
+                v.dh[i][j] = d.dh[i][j];
+                v.dh_inv[i][j] = d.dh_inv[i][j];
+            }
+        }
+        v.ortho = d.ortho ? 1 : 0;
+        if (v.ortho && (d.dh[0][1] != 0.0 || d.dh[0][2] != 0.0 || d.dh[1][0] != 0.0 || d.dh[1][2] != 0.0 ||
+                        d.dh[2][0] != 0.0 || d.dh[2][1] != 0.0 || !(d.dh[0][0] > 0) || !(d.dh[1][1] > 0) ||
+                        !(d.dh[2][2] > 0))) {
+            delete P;
+            return fail(GPW_ERR_INVALID_ARG, "gpw_plan_create: orthorhombic level needs a positive diagonal dh");
+        }
+        v.grid_elems = (int64_t)d.ngrid[0] * d.ngrid[1] * d.ngrid[2];
+        v.tmat_off = -1;
+        if (!v.ortho) {
+            v.tmat_off = (int64_t)tm.size();
+            std::vector<double> T = lattice_transform(v.dh);
+            tm.insert(tm.end(), T.begin(), T.end());
+        }
+    }
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaMalloc(&P->d_levels, sizeof(LevelDev) * nlevels);
+    if (e == cudaSuccess) e = cudaMemcpy(P->d_levels, P->lv, sizeof(LevelDev) * nlevels, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !tm.empty()) {
+        e = cudaMalloc(&P->d_tmat, sizeof(double) * tm.size());
+        if (e == cudaSuccess) e = cudaMemcpy(P->d_tmat, tm.data(), sizeof(double) * tm.size(), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        cudaFree(P->d_levels);
+        cudaFree(P->d_tmat);
+        delete P;
+        return cuda_fail(e, "gpw_plan_create");
+    }
+    P->h_tmat.swap(tm);
+    *plan = P;
+    return GPW_SUCCESS;
+}
+
+int gpw_plan_destroy(gpw_plan *plan) {
+    if (!plan) return GPW_SUCCESS;
+    cudaFree(plan->d_levels);
+    cudaFree(plan->d_tmat);
+    delete plan;
+    return GPW_SUCCESS;
+}
+
+int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, int compute_tau,
+                       const int *sphere_table, int64_t sphere_table_len, gpw_taskset **out) {
+    if (!plan || !out || (ntasks > 0 && !tasks) || ntasks < 0 || ntasks > INT32_MAX)
+        return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_create: bad arguments");
+    *out = nullptr;
+    std::vector<PairGeom> geo((size_t)ntasks);
+    std::vector<int> table;
+    int64_t extent = 0;
+    for (int64_t i = 0; i < ntasks; i++) {
+        int st = make_geom(tasks[i], (int)i, *plan, compute_tau ? 1 : 0, sphere_table, sphere_table_len,
+                           geo[i], table);
+        if (st) return st;
+        const gpw_task &t = tasks[i];
+        const int64_t lo = t.pab_offset + (int64_t)(t.o2 + ncoset(t.lb_min - 1)) * t.maxco + t.o1 + ncoset(t.la_min - 1);
+        const int64_t hi = t.pab_offset + (int64_t)(t.o2 + ncoset(t.lb_max) - 1) * t.maxco + t.o1 + ncoset(t.la_max) - 1;
+        if (lo < 0 || (t.o1 + ncoset(t.la_min - 1)) < 0 || (t.o2 + ncoset(t.lb_min - 1)) < 0) {
+            char buf[128];
+            snprintf(buf, sizeof buf, "task %lld: density block starts before the buffer", (long long)i);
+            return fail(GPW_ERR_INVALID_ARG, buf);
+        }
+        extent = std::max(extent, hi + 1);
+    }
+    // sort: kind (ortho first), then the largest cubes first
+    std::vector<int> order((size_t)ntasks);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        if (geo[a].ortho != geo[b].ortho) return geo[a].ortho > geo[b].ortho;
+        return geo[a].cost > geo[b].cost;
+    });
+    gpw_taskset *T = new gpw_taskset();
+    T->plan = plan;
+    T->tau = compute_tau ? 1 : 0;
+    T->ntasks = ntasks;
+    T->pab_extent = extent;
+    T->h_geom.resize((size_t)ntasks);
+    int64_t coef = 0;
+    for (int64_t k = 0; k < ntasks; k++) {
+        PairGeom g = geo[order[k]];
+        g.coef_off = coef;
+        coef += ncoef(g.lp);
+        T->max_lp = std::max(T->max_lp, g.lp);
+        T->max_A = std::max(T->max_A, g.la_max);
+        T->max_B = std::max(T->max_B, g.lb_max);
+        T->h_geom[k] = g;
+    }
+    T->coef_len = coef;
+    // FP64 launch chunks: similar shared-memory needs launch together
+    int64_t k = 0;
+    int smem_limit = 0;
+    cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, plan->device);
+    while (k < ntasks) {
+        Chunk c;
+        c.first = (int)k;
+        c.kind = T->h_geom[k].ortho ? 0 : 1;
+        c.smem_bytes = 0;
+        int64_t m = k;
+        while (m < ntasks && (T->h_geom[m].ortho ? 0 : 1) == c.kind) {
+            const int need = c.kind == 0 ? smem_ortho_fp64(T->h_geom[m]) : smem_general_fp64(T->h_geom[m]);
+            if (need > smem_limit) {
+                delete T;
+                return fail(GPW_ERR_UNSUPPORTED, "gpw_taskset_create: a cube is too large for one CTA");
+            }
+            if (m > k && need * 2 < c.smem_bytes && m - k >= 64) break;
+            c.smem_bytes = std::max(c.smem_bytes, need);
+            m++;
+        }
+        c.count = (int)(m - k);
+        T->chunks.push_back(c);
+        k = m;
+    }
+    if (smem_prep(T->max_A, T->max_B) > smem_limit) {
+        delete T;
+        return fail(GPW_ERR_UNSUPPORTED, "gpw_taskset_create: angular momenta too high for the set-up kernel");
+    }
+    cudaError_t e = cudaSetDevice(plan->device);
+    auto alloc = [&](void **p, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(p, bytes > 0 ? bytes : 8);
+    };
+    alloc((void **)&T->d_geom, sizeof(PairGeom) * (size_t)ntasks);
+    alloc((void **)&T->d_table, sizeof(int) * table.size());
+    alloc((void **)&T->d_coef, sizeof(double) * (size_t)coef);
+    alloc((void **)&T->d_mom, sizeof(double) * (size_t)coef);
+    alloc((void **)&T->d_status, sizeof(int));
+    if (e == cudaSuccess && ntasks > 0)
+        e = cudaMemcpy(T->d_geom, T->h_geom.data(), sizeof(PairGeom) * (size_t)ntasks, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !table.empty())
+        e = cudaMemcpy(T->d_table, table.data(), sizeof(int) * table.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(T->d_status, 0, sizeof(int));
+    if (e != cudaSuccess) {
+        gpw_taskset_destroy(T);
+        return cuda_fail(e, "gpw_taskset_create");
+    }
+    std::string err;
+    int st = mixed_build(*T, err);
+    if (st) {
+        gpw_taskset_destroy(T);
+        return fail(st, err);
+    }
+    *out = T;
+    return GPW_SUCCESS;
+}
+
+int gpw_taskset_destroy(gpw_taskset *ts) {
+    if (!ts) return GPW_SUCCESS;
+    {
+        std::lock_guard<std::mutex> lk(g_stage_mu);
+        auto it = g_stage.find(ts);
+        if (it != g_stage.end()) {
+            cudaFree(it->second.d_pab);
+            for (int l = 0; l < GPW_MAX_LEVELS; l++) cudaFree(it->second.d_grids[l]);
+            g_stage.erase(it);
+        }
+    }
+    mixed_free(*ts);
+    for (cudaEvent_t e : ts->ev_pool) cudaEventDestroy(e);
+    cudaFree(ts->d_geom);
+    cudaFree(ts->d_table);
+    cudaFree(ts->d_coef);
+    cudaFree(ts->d_mom);
+    cudaFree(ts->d_status);
+    delete ts;
+    return GPW_SUCCESS;
+}
+
+int64_t gpw_taskset_pab_extent(const gpw_taskset *ts) { return ts ? ts->pab_extent : -1; }
+
+int gpw_collocate(gpw_taskset *ts, int precision, const double *d_pab, double *const *d_grids, void *stream) {
+    if (!ts || !d_grids || (ts->ntasks > 0 && !d_pab)) return fail(GPW_ERR_INVALID_ARG, "gpw_collocate: null argument");
+    for (int l = 0; l < ts->plan->nlevels; l++)
+        if (!d_grids[l]) return fail(GPW_ERR_INVALID_ARG, "gpw_collocate: null grid");
+    cudaStream_t s = (cudaStream_t)stream;
+    GridPtrs g = grid_ptrs(*ts->plan, d_grids);
+    GPW_CUDA(launch_prep(*ts, d_pab, s));
+    if (precision == GPW_PREC_FP64) {
+        GPW_CUDA(launch_collocate_fp64(*ts, g, s));
+    } else if (precision == GPW_PREC_MIXED) {
+        GPW_CUDA(launch_collocate_mixed(*ts, g, s));
+    } else {
+        return fail(GPW_ERR_INVALID_ARG, "gpw_collocate: unknown precision");
+    }
+    return GPW_SUCCESS;
+}
+
+int gpw_integrate(gpw_taskset *ts, int precision, double *const *d_grids, double *d_hab, void *stream) {
+    if (!ts || !d_grids || (ts->ntasks > 0 && !d_hab)) return fail(GPW_ERR_INVALID_ARG, "gpw_integrate: null argument");
+    for (int l = 0; l < ts->plan->nlevels; l++)
+        if (!d_grids[l]) return fail(GPW_ERR_INVALID_ARG, "gpw_integrate: null grid");
+    cudaStream_t s = (cudaStream_t)stream;
+    GridPtrs g = grid_ptrs(*ts->plan, d_grids);
+    if (precision == GPW_PREC_FP64) {
+        GPW_CUDA(launch_integrate_fp64(*ts, g, s));
+    } else if (precision == GPW_PREC_MIXED) {
+        GPW_CUDA(launch_integrate_mixed(*ts, g, s));
+    } else {
+        return fail(GPW_ERR_INVALID_ARG, "gpw_integrate: unknown precision");
+    }
+    GPW_CUDA(launch_backtransform(*ts, ts->d_mom, d_hab, s));
+    return GPW_SUCCESS;
+}
+
+int gpw_backward(gpw_taskset *ts, const double *d_pab, double *const *d_grids, double *d_hab, double *d_dra,
+                 double *d_drb, double *d_dzeta, double *d_dzetb, void *stream) {
+    if (!ts || !d_grids || (ts->ntasks > 0 && !d_pab)) return fail(GPW_ERR_INVALID_ARG, "gpw_backward: null argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    GridPtrs g = grid_ptrs(*ts->plan, d_grids);
+    if (d_hab) {
+        int st = gpw_integrate(ts, GPW_PREC_FP64, d_grids, d_hab, stream);
+        if (st) return st;
+    }
+    if (d_dra || d_drb || d_dzeta || d_dzetb) {
+        cudaError_t e = launch_backward(*ts, d_pab, g, d_hab, d_dra, d_drb, d_dzeta, d_dzetb, s);
+        if (e == cudaErrorNotSupported) return fail(GPW_ERR_UNSUPPORTED, "gpw_backward: not available");
+        if (e != cudaSuccess) return cuda_fail(e, "gpw_backward");
+    }
+    return GPW_SUCCESS;
+}
+
+int gpw_taskset_check(gpw_taskset *ts, void *stream) {
+    if (!ts) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_check: null");
+    int h = 0;
+    GPW_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    GPW_CUDA(cudaMemcpy(&h, ts->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    GPW_CUDA(cudaMemset(ts->d_status, 0, sizeof(int)));
+    if (h & kStatOutOfWindow) return fail(GPW_ERR_OUT_OF_WINDOW, "a cube left the local grid window");
+    if (h & kStatTimeout) return fail(GPW_ERR_TIMEOUT, "a bounded device wait gave up");
+    if (h & kStatBadTable) return fail(GPW_ERR_INVALID_ARG, "a cube list was inconsistent on the device");
+    return GPW_SUCCESS;
+}
+
+int gpw_taskset_profile(gpw_taskset *ts, int enable) {
+    if (!ts) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_profile: null");
+    ts->profile = enable != 0;
+    return GPW_SUCCESS;
+}
+
+int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms, int64_t *contraction_launches,
+                      int64_t *kernel_launches) {
+    if (!ts) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_stats: null");
+    double ms = 0.0;
+    if (ts->ev_used > 0) {
+        GPW_CUDA(cudaEventSynchronize(ts->ev_pool[ts->ev_used - 1]));
+        for (size_t i = 0; i + 1 < ts->ev_used; i += 2) {
+            float m = 0.f;
+            GPW_CUDA(cudaEventElapsedTime(&m, ts->ev_pool[i], ts->ev_pool[i + 1]));
+            ms += m;
+        }
+    }
+    if (contraction_ms) *contraction_ms = ms;
+    if (contraction_launches) *contraction_launches = ts->n_contract;
+    if (kernel_launches) *kernel_launches = ts->n_kernels;
+    ts->ev_used = 0;
+    ts->n_contract = 0;
+    ts->n_kernels = 0;
+    return GPW_SUCCESS;
+}
+
+static int stage(gpw_taskset *ts, HostStage **out) {
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    HostStage &h = g_stage[ts];
+    cudaError_t e = cudaSuccess;
+    if (!h.d_pab) {
+        e = cudaMalloc(&h.d_pab, sizeof(double) * std::max<int64_t>(ts->pab_extent, 1));
+        for (int l = 0; l < ts->plan->nlevels && e == cudaSuccess; l++)
+            e = cudaMalloc(&h.d_grids[l], sizeof(double) * ts->plan->lv[l].grid_elems);
+        if (e != cudaSuccess) return cuda_fail(e, "host staging");
+    }
+    *out = &h;
+    return GPW_SUCCESS;
+}
+
+int gpw_collocate_host(gpw_taskset *ts, int precision, const double *h_pab, double *const *h_grids) {
+    if (!ts || !h_grids || (ts->ntasks > 0 && !h_pab)) return fail(GPW_ERR_INVALID_ARG, "gpw_collocate_host: null");
+    GPW_CUDA(cudaSetDevice(ts->plan->device));
+    HostStage *h;
+    int st = stage(ts, &h);
+    if (st) return st;
+    GPW_CUDA(cudaMemcpy(h->d_pab, h_pab, sizeof(double) * ts->pab_extent, cudaMemcpyHostToDevice));
+    for (int l = 0; l < ts->plan->nlevels; l++)
+        GPW_CUDA(cudaMemcpy(h->d_grids[l], h_grids[l], sizeof(double) * ts->plan->lv[l].grid_elems,
+                            cudaMemcpyHostToDevice));
+    st = gpw_collocate(ts, precision, h->d_pab, h->d_grids, nullptr);
+    if (st) return st;
+    for (int l = 0; l < ts->plan->nlevels; l++)
+        GPW_CUDA(cudaMemcpy(h_grids[l], h->d_grids[l], sizeof(double) * ts->plan->lv[l].grid_elems,
+                            cudaMemcpyDeviceToHost));
+    return gpw_taskset_check(ts, nullptr);
+}
+
+int gpw_integrate_host(gpw_taskset *ts, int precision, double *const *h_grids, double *h_hab) {
+    if (!ts || !h_grids || (ts->ntasks > 0 && !h_hab)) return fail(GPW_ERR_INVALID_ARG, "gpw_integrate_host: null");
+    GPW_CUDA(cudaSetDevice(ts->plan->device));
+    HostStage *h;
+    int st = stage(ts, &h);
+    if (st) return st;
+    for (int l = 0; l < ts->plan->nlevels; l++)
+        GPW_CUDA(cudaMemcpy(h->d_grids[l], h_grids[l], sizeof(double) * ts->plan->lv[l].grid_elems,
+                            cudaMemcpyHostToDevice));
+    GPW_CUDA(cudaMemcpy(h->d_pab, h_hab, sizeof(double) * ts->pab_extent, cudaMemcpyHostToDevice));
+    st = gpw_integrate(ts, precision, h->d_grids, h->d_pab, nullptr);
+    if (st) return st;
+    GPW_CUDA(cudaMemcpy(h_hab, h->d_pab, sizeof(double) * ts->pab_extent, cudaMemcpyDeviceToHost));
+    return gpw_taskset_check(ts, nullptr);
+}
+
+int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max, int la_min, int lb_max,
+                                     int lb_min, double zeta, double zetb, double rscale, const double dh[3][3],
+                                     const double dh_inv[3][3], const double ra[3], const double rab[3],
+                                     const int npts[3], const int ngrid[3], const int lb_grid[3],
+                                     const int periodic[3], int lmax, double radius, const int lb_cube[3],
+                                     const int ub_cube[3], int nspheres, const int *sphere_bounds, int maxco,
+                                     int o1, int o2, const double *pab, double *grid) {
+    (void)lmax;
+    if (!dh || !dh_inv || !ra || !rab || !npts || !ngrid || !lb_grid || !periodic || !pab || !grid)
+        return fail(GPW_ERR_INVALID_ARG, "gpw_collocate_pgf_product_rspace: null argument");
+    if (use_ortho && (!lb_cube || !ub_cube || !sphere_bounds || nspheres < 1))
+        return fail(GPW_ERR_INVALID_ARG, "gpw_collocate_pgf_product_rspace: ortho needs the cube and its list");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    gpw_grid_desc gd;
+    memset(&gd, 0, sizeof gd);
+    for (int i = 0; i < 3; i++) {
+        gd.npts[i] = npts[i];
+        gd.ngrid[i] = ngrid[i];
+        gd.lb_grid[i] = lb_grid[i];
+        gd.periodic[i] = periodic[i];
+        for (int j = 0; j < 3; j++) {
+            gd.dh[i][j] = dh[i][j];
+            gd.dh_inv[i][j] = dh_inv[i][j];
+        }
+    }
+    gd.ortho = use_ortho ? 1 : 0;
+    gpw_plan *P = nullptr;
+    int st = gpw_plan_create(&P, 1, &gd, dev);
+    if (st) return st;
+    gpw_task t;
+    memset(&t, 0, sizeof t);
+    t.zeta = zeta; t.zetb = zetb; t.rscale = rscale;
+    for (int i = 0; i < 3; i++) { t.ra[i] = ra[i]; t.rab[i] = rab[i]; }
+    t.radius = radius;
+    t.pab_offset = 0;
+    t.la_max = la_max; t.la_min = la_min; t.lb_max = lb_max; t.lb_min = lb_min;
+    t.level = 0; t.maxco = maxco; t.o1 = o1; t.o2 = o2;
+    t.sphere_offset = use_ortho ? 0 : -1;
+    if (use_ortho)
+        for (int i = 0; i < 3; i++) { t.lb_cube[i] = lb_cube[i]; t.ub_cube[i] = ub_cube[i]; }
+    gpw_taskset *T = nullptr;
+    st = gpw_taskset_create(P, &t, 1, compute_tau, use_ortho ? sphere_bounds : nullptr,
+                            use_ortho ? nspheres : 0, &T);
+    if (st == GPW_SUCCESS) {
+        // the block is read at (o2+jco)*maxco + o1+ico < maxco*maxco
+        double *gp[1] = {grid};
+        std::vector<double> blk(pab, pab + (size_t)maxco * maxco);
+        if (T->pab_extent > (int64_t)blk.size()) blk.resize((size_t)T->pab_extent, 0.0);
+        st = gpw_collocate_host(T, GPW_PREC_FP64, blk.data(), gp);
+    }
+    gpw_taskset_destroy(T);
+    gpw_plan_destroy(P);
+    return st;
+}
+
+int gpw_collocate_core(const int length[3], int L, const double *d_co, const double *d_pol, int ld_pol,
+                       double *d_out, void *stream) {
+    if (!length || L < 1 || L > 16 || !d_co || !d_pol || !d_out || ld_pol < std::max({length[0], length[1], length[2]}))
+        return fail(GPW_ERR_INVALID_ARG, "gpw_collocate_core: bad arguments");
+    GPW_CUDA(launch_collocate_core(length, L, d_co, d_pol, ld_pol, d_out, (cudaStream_t)stream));
+    return GPW_SUCCESS;
+}
+
+int gpw_integrate_core(const int length[3], int L, const double *d_pol, int ld_pol, const double *d_V,
+                       double *d_co, void *stream) {
+    if (!length || L < 1 || L > 16 || !d_co || !d_pol || !d_V || ld_pol < std::max({length[0], length[1], length[2]}))
+        return fail(GPW_ERR_INVALID_ARG, "gpw_integrate_core: bad arguments");
+    GPW_CUDA(launch_integrate_core(length, L, d_pol, ld_pol, d_V, d_co, (cudaStream_t)stream));
+    return GPW_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,274 @@
+// Pair coefficient transforms on the device, FP64, one CTA per pair.
+//
+// Forward (collocate set-up), following grid_base_ref_c.cc:849-979:
+//   density block  -> local block P(b,a)     rho: grid_base_ref_c.cc:158-192
+//                                             tau: grid_base_ref_c.cc:65-155
+//   1-D re-centring (x-a)^i (x-b)^j = sum_k al[i][j][k] (x-p)^k   :195-231
+//   P -> c[lz][ly][lx] by three one-axis contractions              :234-315
+// Adjoint (integrate back-transform): the same three contractions transposed,
+// then the transposed block map, accumulated into the caller's hab.
+#pragma once
+
+#include "gpw_common.cuh"
+
+namespace gpw {
+
+GPW_HD void coset_decode(int ico, int &lx, int &ly, int &lz) {
+    int l = 0;
+    while (ncoset(l) <= ico) l++;
+    int s = ico - ncoset(l - 1);
+    // s = ((l-lx)(l-lx+1))/2 + lz, 0 <= lz <= l-lx
+    lx = l;
+    while (((l - lx) * (l - lx + 1)) / 2 + (l - lx) < s) lx--;
+    lz = s - ((l - lx) * (l - lx + 1)) / 2;
+    ly = l - lx - lz;
+}
+
+// (ly, lz) with ly + lz <= A, packed
+GPW_HD int tri(int ly, int lz) { return ((ly + lz) * (ly + lz + 1)) / 2 + lz; }
+GPW_HD void tri_decode(int t, int &ly, int &lz) {
+    int s = 0;
+    while (((s + 1) * (s + 2)) / 2 <= t) s++;
+    lz = t - (s * (s + 1)) / 2;
+    ly = s - lz;
+}
+
+struct CoefDims {
+    int A, B, L;      // local la_max, lb_max, lp + 1
+    int nla, nlb;     // ncoset(A), ncoset(B)
+    int na2, nb2;     // (A+1)(A+2)/2, (B+1)(B+2)/2
+    GPW_HD void set(int A_, int B_) {
+        A = A_; B = B_; L = A + B + 1;
+        nla = ncoset(A); nlb = ncoset(B);
+        na2 = nshell(A); nb2 = nshell(B);
+    }
+    GPW_HD int n_P() const { return nla * nlb; }
+    GPW_HD int n_al() const { return 3 * (A + 1) * (B + 1) * L; }
+    GPW_HD int n_T1() const { return na2 * nb2 * L; }
+    GPW_HD int n_T2() const { return (A + 1) * (B + 1) * L * L; }
+    GPW_HD int n_total() const { return n_P() + n_al() + n_T1() + n_T2(); }
+};
+
+// Shared-memory doubles a CTA needs for pairs up to la, lb (local, after tau).
+GPW_HD int coef_ws_doubles(int A, int B) {
+    CoefDims d;
+    d.set(A, B);
+    return d.n_total();
+}
+
+struct CoefWs {
+    CoefDims d;
+    double *P, *al, *T1, *T2;
+    __device__ void carve(double *base, int A, int B) {
+        d.set(A, B);
+        P = base;
+        al = P + d.n_P();
+        T1 = al + d.n_al();
+        T2 = T1 + d.n_T1();
+    }
+    __device__ double &AL(int ax, int i, int j, int k) {
+        return al[((ax * (d.A + 1) + i) * (d.B + 1) + j) * d.L + k];
+    }
+};
+
+__device__ inline void fill_alpha(CoefWs &w, const PairGeom &g) {
+    const int n = 3 * (w.d.A + 1) * (w.d.B + 1);
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int j = t % (w.d.B + 1);
+        const int i = (t / (w.d.B + 1)) % (w.d.A + 1);
+        const int ax = t / ((w.d.B + 1) * (w.d.A + 1));
+        const double pa = g.rp[ax] - g.ra[ax];
+        const double pb = g.rp[ax] - g.rb[ax];
+        double *out = &w.AL(ax, i, j, 0);
+        for (int k = 0; k < w.d.L; k++) out[k] = 0.0;
+        double ci = 1.0;  // C(i, k1)
+        for (int k1 = 0; k1 <= i; k1++) {
+            double pai = 1.0;
+            for (int e = 0; e < i - k1; e++) pai *= pa;
+            double cj = 1.0;
+            for (int k2 = 0; k2 <= j; k2++) {
+                double pbj = 1.0;
+                for (int e = 0; e < j - k2; e++) pbj *= pb;
+                out[k1 + k2] += ci * pai * cj * pbj;
+                cj = cj * (double)(j - k2) / (double)(k2 + 1);
+            }
+            ci = ci * (double)(i - k1) / (double)(k1 + 1);
+        }
+    }
+}
+
+__device__ inline int64_t block_index(const PairGeom &g, int jco, int ico) {
+    return g.pab_offset + (int64_t)(g.o2 + jco) * g.maxco + (g.o1 + ico);
+}
+
+// P(b', a') of the local block (rho copy or tau gradient products).
+__device__ inline void fill_local_block(CoefWs &w, const PairGeom &g, int tau, const double *pab) {
+    const int n = w.d.n_P();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int jco = t / w.d.nla, ico = t % w.d.nla;
+        int a[3], b[3];
+        coset_decode(ico, a[0], a[1], a[2]);
+        coset_decode(jco, b[0], b[1], b[2]);
+        const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
+        double v = 0.0;
+        if (!tau) {
+            if (la >= g.la0_min && la <= g.la0_max && lb >= g.lb0_min && lb <= g.lb0_max)
+                v = pab[block_index(g, jco, ico)];
+        } else {
+            for (int d = 0; d < 3; d++)
+                for (int sa = 0; sa < 2; sa++) {
+                    int as[3] = {a[0], a[1], a[2]};
+                    double ca;
+                    if (sa == 0) { as[d] += 1; ca = (double)as[d]; }       // source lowered to a'
+                    else { if (a[d] == 0) continue; as[d] -= 1; ca = -2.0 * g.zeta; }  // source raised
+                    const int las = as[0] + as[1] + as[2];
+                    if (las < g.la0_min || las > g.la0_max) continue;
+                    for (int sb = 0; sb < 2; sb++) {
+                        int bs[3] = {b[0], b[1], b[2]};
+                        double cb;
+                        if (sb == 0) { bs[d] += 1; cb = (double)bs[d]; }
+                        else { if (b[d] == 0) continue; bs[d] -= 1; cb = -2.0 * g.zetb; }
+                        const int lbs = bs[0] + bs[1] + bs[2];
+                        if (lbs < g.lb0_min || lbs > g.lb0_max) continue;
+                        v += 0.5 * ca * cb *
+                             pab[block_index(g, coset(bs[0], bs[1], bs[2]), coset(as[0], as[1], as[2]))];
+                    }
+                }
+        }
+        w.P[t] = v;
+    }
+}
+
+// c (packed, prefactor included) from P.  Writes packed coefficients to `out`.
+__device__ inline void forward_coef(CoefWs &w, const PairGeom &g, double *out) {
+    const CoefDims &d = w.d;
+    const int L = d.L;
+    // X: T1[ta][tb][lx] = sum_{lxa,lxb} P[b][a] al_x[lxa][lxb][lx]
+    for (int t = threadIdx.x; t < d.n_T1(); t += blockDim.x) {
+        const int lx = t % L;
+        const int tb = (t / L) % d.nb2;
+        const int ta = t / (L * d.nb2);
+        int lya, lza, lyb, lzb;
+        tri_decode(ta, lya, lza);
+        tri_decode(tb, lyb, lzb);
+        double s = 0.0;
+        const int xa0 = max(g.la_min - lya - lza, 0), xa1 = g.la_max - lya - lza;
+        const int xb0 = max(g.lb_min - lyb - lzb, 0), xb1 = g.lb_max - lyb - lzb;
+        for (int lxa = xa0; lxa <= xa1; lxa++)
+            for (int lxb = xb0; lxb <= xb1; lxb++) {
+                if (lx > lxa + lxb) continue;
+                s += w.P[coset(lxb, lyb, lzb) * d.nla + coset(lxa, lya, lza)] * w.AL(0, lxa, lxb, lx);
+            }
+        w.T1[t] = s;
+    }
+    __syncthreads();
+    // Y: T2[lza][lzb][ly][lx] = sum_{lya,lyb} T1[(lya,lza)][(lyb,lzb)][lx] al_y[lya][lyb][ly]
+    for (int t = threadIdx.x; t < d.n_T2(); t += blockDim.x) {
+        const int lx = t % L;
+        const int ly = (t / L) % L;
+        const int lzb = (t / (L * L)) % (d.B + 1);
+        const int lza = t / (L * L * (d.B + 1));
+        double s = 0.0;
+        for (int lya = 0; lya <= d.A - lza; lya++)
+            for (int lyb = 0; lyb <= d.B - lzb; lyb++) {
+                if (ly > lya + lyb) continue;
+                s += w.T1[(tri(lya, lza) * d.nb2 + tri(lyb, lzb)) * L + lx] * w.AL(1, lya, lyb, ly);
+            }
+        w.T2[t] = s;
+    }
+    __syncthreads();
+    // Z: c[lz][ly][lx] = pref * sum_{lza,lzb} T2[lza][lzb][ly][lx] al_z[lza][lzb][lz]
+    const int lp = g.lp;
+    for (int t = threadIdx.x; t < L * L * L; t += blockDim.x) {
+        const int lx = t % L, ly = (t / L) % L, lz = t / (L * L);
+        if (lx + ly + lz > lp) continue;
+        double s = 0.0;
+        for (int lza = 0; lza <= d.A; lza++)
+            for (int lzb = 0; lzb <= d.B; lzb++) {
+                if (lz > lza + lzb) continue;
+                s += w.T2[((lza * (d.B + 1) + lzb) * L + ly) * L + lx] * w.AL(2, lza, lzb, lz);
+            }
+        out[pidx(lp, lz, ly, lx)] = g.prefactor * s;
+    }
+}
+
+// Adjoint: given moments W (packed like c), accumulate into hab.
+__device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int tau, const double *W,
+                                    double *hab) {
+    const CoefDims &d = w.d;
+    const int L = d.L, lp = g.lp;
+    // Z^T: T2[lza][lzb][ly][lx] = sum_lz al_z[lza][lzb][lz] W[lz][ly][lx]
+    for (int t = threadIdx.x; t < d.n_T2(); t += blockDim.x) {
+        const int lx = t % L;
+        const int ly = (t / L) % L;
+        const int lzb = (t / (L * L)) % (d.B + 1);
+        const int lza = t / (L * L * (d.B + 1));
+        double s = 0.0;
+        for (int lz = 0; lz <= lza + lzb && lz + ly + lx <= lp; lz++)
+            s += w.AL(2, lza, lzb, lz) * W[pidx(lp, lz, ly, lx)];
+        w.T2[t] = s;
+    }
+    __syncthreads();
+    // Y^T: T1[ta][tb][lx] = sum_ly al_y[lya][lyb][ly] T2[lza][lzb][ly][lx]
+    for (int t = threadIdx.x; t < d.n_T1(); t += blockDim.x) {
+        const int lx = t % L;
+        const int tb = (t / L) % d.nb2;
+        const int ta = t / (L * d.nb2);
+        int lya, lza, lyb, lzb;
+        tri_decode(ta, lya, lza);
+        tri_decode(tb, lyb, lzb);
+        double s = 0.0;
+        for (int ly = 0; ly <= lya + lyb; ly++)
+            s += w.AL(1, lya, lyb, ly) * w.T2[((lza * (d.B + 1) + lzb) * L + ly) * L + lx];
+        w.T1[t] = s;
+    }
+    __syncthreads();
+    // X^T: P[b][a] = pref * sum_lx al_x[lxa][lxb][lx] T1[(lya,lza)][(lyb,lzb)][lx]
+    for (int t = threadIdx.x; t < d.n_P(); t += blockDim.x) {
+        const int jco = t / d.nla, ico = t % d.nla;
+        int a[3], b[3];
+        coset_decode(ico, a[0], a[1], a[2]);
+        coset_decode(jco, b[0], b[1], b[2]);
+        const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
+        double s = 0.0;
+        if (la >= g.la_min && la <= g.la_max && lb >= g.lb_min && lb <= g.lb_max) {
+            const int ta = tri(a[1], a[2]), tb = tri(b[1], b[2]);
+            for (int lx = 0; lx <= a[0] + b[0]; lx++)
+                s += w.AL(0, a[0], b[0], lx) * w.T1[(ta * d.nb2 + tb) * L + lx];
+        }
+        w.P[t] = g.prefactor * s;
+    }
+    __syncthreads();
+    // block map transposed, into hab (pairs may share hab entries: atomics)
+    const int na0 = ncoset(g.la0_max), nb0 = ncoset(g.lb0_max);
+    for (int t = threadIdx.x; t < na0 * nb0; t += blockDim.x) {
+        const int jco = t / na0, ico = t % na0;
+        int a[3], b[3];
+        coset_decode(ico, a[0], a[1], a[2]);
+        coset_decode(jco, b[0], b[1], b[2]);
+        const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
+        if (la < g.la0_min || la > g.la0_max || lb < g.lb0_min || lb > g.lb0_max) continue;
+        double s = 0.0;
+        if (!tau) {
+            s = w.P[jco * d.nla + ico];
+        } else {
+            for (int dd = 0; dd < 3; dd++)
+                for (int sa = 0; sa < 2; sa++) {
+                    int at[3] = {a[0], a[1], a[2]};
+                    double ca;
+                    if (sa == 0) { if (a[dd] == 0) continue; ca = (double)a[dd]; at[dd] -= 1; }
+                    else { ca = -2.0 * g.zeta; at[dd] += 1; }
+                    for (int sb = 0; sb < 2; sb++) {
+                        int bt[3] = {b[0], b[1], b[2]};
+                        double cb;
+                        if (sb == 0) { if (b[dd] == 0) continue; cb = (double)b[dd]; bt[dd] -= 1; }
+                        else { cb = -2.0 * g.zetb; bt[dd] += 1; }
+                        s += 0.5 * ca * cb * w.P[coset(bt[0], bt[1], bt[2]) * d.nla + coset(at[0], at[1], at[2])];
+                    }
+                }
+        }
+        atomicAdd(&hab[block_index(g, jco, ico)], s);
+    }
+}
+
+}  // namespace gpw

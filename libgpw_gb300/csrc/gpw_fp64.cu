@@ -1,0 +1,538 @@
+// Plain FP64 collocate / integrate: one CTA per pair, FP64 everywhere, grid
+// updates by FP64 atomics.  This is the straightforward GPU form of the
+// reference's per-pair loops (grid_collocate_core, grid_base_ref_c.cc:403-508;
+// grid_collocate_general, :593-846) and the denominator the tiled path is
+// measured against.
+#include <cuda_runtime.h>
+
+#include "gpw_coef.cuh"
+#include "gpw_internal.h"
+
+namespace gpw {
+
+// ---------------------------------------------------------------------------
+// cube lists: sphere rule or explicit (random-access) table
+// table layout at g.table_off: kgmin, then (jgmin, rowstart) per kf, then igmin per row
+__device__ __forceinline__ int cube_jgmin(const PairGeom &g, const LevelDev &lv, const int *table,
+                                          int kf, double r2, double &remk) {
+    if (g.table_off < 0) {
+        remk = rule_remk(r2, kf, lv.dh[2][2]);
+        return -rule_jmax(remk, lv.dh[1][1]);
+    }
+    const int *T = table + g.table_off;
+    remk = 0.0;
+    return T[1 + 2 * (kf - T[0])];
+}
+__device__ __forceinline__ int cube_igmin(const PairGeom &g, const LevelDev &lv, const int *table,
+                                          int kf, int jf, int jgmin, double remk) {
+    if (g.table_off < 0) return -rule_imax(remk, jf, lv.dh[1][1], lv.dh[0][0]);
+    const int *T = table + g.table_off;
+    const int nk = 1 - T[0];
+    return T[1 + 2 * nk + T[2 + 2 * (kf - T[0])] + (jf - jgmin)];
+}
+
+// 1-D tables tab[k][gi] = t^k exp(-zetp t^2), t = (lo+gi)*h - off, k < L  (grid_fill_pol,
+// grid_base_ref_c.cc:355-400; evaluated directly instead of by recurrence)
+__device__ __forceinline__ void fill_table(double *tab, int n, int L, int lo, double h, double off,
+                                           double zetp) {
+    for (int gi = threadIdx.x; gi < n; gi += blockDim.x) {
+        const double t = (double)(lo + gi) * h - off;
+        double e = exp(-zetp * t * t);
+        for (int k = 0; k < L; k++) {
+            tab[k * n + gi] = e;
+            e *= t;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// pair set-up: packed coefficients c (ortho) or q (general, lattice basis)
+__global__ void k_prep(const PairGeom *__restrict__ geoms, const LevelDev *__restrict__ levels,
+                       const double *__restrict__ tmat, int tau, const double *__restrict__ pab,
+                       double *__restrict__ coef) {
+    extern __shared__ double sm[];
+    const PairGeom g = geoms[blockIdx.x];
+    CoefWs w;
+    w.carve(sm, g.la_max, g.lb_max);
+    fill_alpha(w, g);
+    fill_local_block(w, g, tau, pab);
+    __syncthreads();
+    const int nc = ncoef(g.lp);
+    if (g.ortho) {
+        forward_coef(w, g, coef + g.coef_off);
+        return;
+    }
+    double *c = w.T2 + w.d.n_T2();  // packed c, before the lattice transform
+    forward_coef(w, g, c);
+    __syncthreads();
+    // q[k][j][i] = sum over same-degree (lz,ly,lx) of T * c; T in lp = kMaxLp packing
+    const LevelDev &lv = levels[g.level];
+    const double *Tm = tmat + lv.tmat_off;
+    const int NT = ncoef(kMaxLp);
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+        // decode t -> (k, j, i) in lp packing
+        int k = 0, j = 0, i = 0;
+        {
+            int r = t;
+            for (k = 0; k <= g.lp; k++) {
+                const int cnt = ((g.lp - k + 1) * (g.lp - k + 2)) / 2;
+                if (r < cnt) break;
+                r -= cnt;
+            }
+            const int q = g.lp - k;
+            for (j = 0; j <= q; j++) {
+                if (r <= q - j) break;
+                r -= q - j + 1;
+            }
+            i = r;
+        }
+        const int n = i + j + k;
+        const int row = pidx(kMaxLp, k, j, i);
+        double s = 0.0;
+        for (int lz = 0; lz <= n; lz++)
+            for (int ly = 0; ly <= n - lz; ly++) {
+                const int lx = n - lz - ly;
+                s += Tm[(int64_t)row * NT + pidx(kMaxLp, lz, ly, lx)] * c[pidx(g.lp, lz, ly, lx)];
+            }
+        coef[g.coef_off + t] = s;
+    }
+}
+
+int smem_prep(int A, int B) {
+    // workspace + a packed coefficient vector for the general-cell transform
+    return 8 * (coef_ws_doubles(A, B) + ncoef(A + B));
+}
+
+// ---------------------------------------------------------------------------
+// integrate back-transform: moments -> hab
+__global__ void k_backtransform(const PairGeom *__restrict__ geoms, const LevelDev *__restrict__ levels,
+                                const double *__restrict__ tmat, int tau,
+                                const double *__restrict__ mom, double *__restrict__ hab) {
+    extern __shared__ double sm[];
+    const PairGeom g = geoms[blockIdx.x];
+    CoefWs w;
+    w.carve(sm, g.la_max, g.lb_max);
+    fill_alpha(w, g);
+    const int nc = ncoef(g.lp);
+    const double *W = mom + g.coef_off;
+    double *Wc = w.T2 + w.d.n_T2();
+    if (!g.ortho) {
+        // Wc[lz][ly][lx] = sum over same-degree (k,j,i) of T[(k,j,i)][(lz,ly,lx)] * Wq[k][j][i]
+        const LevelDev &lv = levels[g.level];
+        const double *Tm = tmat + lv.tmat_off;
+        const int NT = ncoef(kMaxLp);
+        for (int t = threadIdx.x; t < nc; t += blockDim.x) {
+            int lz = 0, ly = 0, lx = 0;
+            int r = t;
+            for (lz = 0; lz <= g.lp; lz++) {
+                const int cnt = ((g.lp - lz + 1) * (g.lp - lz + 2)) / 2;
+                if (r < cnt) break;
+                r -= cnt;
+            }
+            const int q = g.lp - lz;
+            for (ly = 0; ly <= q; ly++) {
+                if (r <= q - ly) break;
+                r -= q - ly + 1;
+            }
+            lx = r;
+            const int n = lx + ly + lz;
+            const int col = pidx(kMaxLp, lz, ly, lx);
+            double s = 0.0;
+            for (int k = 0; k <= n; k++)
+                for (int j = 0; j <= n - k; j++) {
+                    const int i = n - k - j;
+                    s += Tm[(int64_t)pidx(kMaxLp, k, j, i) * NT + col] * W[pidx(g.lp, k, j, i)];
+                }
+            Wc[t] = s;
+        }
+        W = Wc;
+    }
+    __syncthreads();
+    adjoint_coef(w, g, tau, W, hab);
+}
+
+// ---------------------------------------------------------------------------
+// orthorhombic collocate, one CTA per pair
+int smem_ortho_fp64(const PairGeom &g) {
+    const int L = g.lp + 1;
+    const int nx = g.hi[0] - g.lb[0] + 1, ny = g.hi[1] - g.lb[1] + 1, nz = g.hi[2] - g.lb[2] + 1;
+    return 8 * (L * L * L + L * (nx + ny + nz) + L * L + ny * L) + 8 * ny;
+}
+
+template <bool kAdj>
+__global__ void __launch_bounds__(256)
+k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__restrict__ levels,
+             const int *__restrict__ table, const double *__restrict__ coef, double *__restrict__ mom,
+             GridPtrs grids, int *status) {
+    extern __shared__ double sm[];
+    const PairGeom g = geoms[first + blockIdx.x];
+    const LevelDev &lv = levels[g.level];
+    double *__restrict__ grid = grids.p[g.level];
+    const int lp = g.lp, L = lp + 1;
+    const int nx = g.hi[0] - g.lb[0] + 1, ny = g.hi[1] - g.lb[1] + 1, nz = g.hi[2] - g.lb[2] + 1;
+    double *C = sm;                // [lz][ly][lx] dense: coefficients, or moments (adjoint)
+    double *Xt = C + L * L * L;    // [k][gi]
+    double *Yt = Xt + L * nx;
+    double *Zt = Yt + L * ny;
+    double *Cxy = Zt + L * nz;     // [ly][lx]
+    double *Cx = Cxy + L * L;      // [row][lx]
+    int *rows = (int *)(Cx + ny * L);  // per row: igmin, j
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    for (int t = tid; t < L * L * L; t += nthr) {
+        const int lx = t % L, ly = (t / L) % L, lz = t / (L * L);
+        C[t] = (!kAdj && lx + ly + lz <= lp) ? coef[g.coef_off + pidx(lp, lz, ly, lx)] : 0.0;
+    }
+    fill_table(Xt, nx, L, g.lb[0], lv.dh[0][0], g.off[0], g.zetp);
+    fill_table(Yt, ny, L, g.lb[1], lv.dh[1][1], g.off[1], g.zetp);
+    fill_table(Zt, nz, L, g.lb[2], lv.dh[2][2], g.off[2], g.zetp);
+    __syncthreads();
+    const double r2 = rmul(g.radius, g.radius);
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+    for (int kg = g.kgmin; kg <= 1 - g.kgmin; kg++) {
+        const int kf = fold(kg);
+        const int k = axis_index(lv.periodic[2], g.cc[2], kg, g.lb[2], lv.lb_grid[2], lv.npts[2],
+                                 lv.ngrid[2]);
+        if (k < 0) {
+            if (tid == 0) atomicOr(status, kStatOutOfWindow);
+            continue;
+        }
+        double remk;
+        const int jgmin = cube_jgmin(g, lv, table, kf, r2, remk);
+        const int nrows = 2 - 2 * jgmin;
+        const double *Zk = Zt + (kg - g.lb[2]);
+        if (!kAdj) {
+            // Cxy[ly][lx] = sum_lz C[lz][ly][lx] Z[lz]
+            for (int t = tid; t < L * L; t += nthr) {
+                const int lx = t % L, ly = t / L;
+                double s = 0.0;
+                for (int lz = 0; lz <= lp - lx - ly; lz++) s += C[(lz * L + ly) * L + lx] * Zk[lz * nz];
+                Cxy[t] = s;
+            }
+            __syncthreads();
+        }
+        for (int t = tid; t < nrows * L; t += nthr) {
+            const int row = t / L, lx = t % L;
+            const int jg = jgmin + row;
+            if (!kAdj) {
+                double s = 0.0;
+                for (int ly = 0; ly <= lp - lx; ly++) s += Cxy[ly * L + lx] * Yt[ly * ny + (jg - g.lb[1])];
+                Cx[t] = s;
+            }
+            if (lx == 0) {
+                rows[2 * row] = cube_igmin(g, lv, table, kf, fold(jg), jgmin, remk);
+                rows[2 * row + 1] = axis_index(lv.periodic[1], g.cc[1], jg, g.lb[1], lv.lb_grid[1],
+                                               lv.npts[1], lv.ngrid[1]);
+            }
+        }
+        __syncthreads();
+        for (int row = warp; row < nrows; row += nwarp) {
+            const int igmin = rows[2 * row], j = rows[2 * row + 1];
+            if (j < 0) {
+                if (lane == 0) atomicOr(status, kStatOutOfWindow);
+                continue;
+            }
+            const int64_t rowbase = ((int64_t)k * lv.ngrid[1] + j) * lv.ngrid[0];
+            double acc[kNPow];
+#pragma unroll
+            for (int lx = 0; lx < kNPow; lx++) acc[lx] = 0.0;
+            for (int ig = igmin + lane; ig <= 1 - igmin; ig += 32) {
+                const int i = axis_index(lv.periodic[0], g.cc[0], ig, g.lb[0], lv.lb_grid[0],
+                                         lv.npts[0], lv.ngrid[0]);
+                if (i < 0) {
+                    atomicOr(status, kStatOutOfWindow);
+                    continue;
+                }
+                const double *Xi = Xt + (ig - g.lb[0]);
+                if (!kAdj) {
+                    double v = 0.0;
+                    for (int lx = 0; lx < L; lx++) v += Cx[row * L + lx] * Xi[lx * nx];
+                    atomicAdd(grid + rowbase + i, v);
+                } else {
+                    const double v = grid[rowbase + i];
+#pragma unroll
+                    for (int lx = 0; lx < kNPow; lx++)
+                        if (lx < L) acc[lx] += v * Xi[lx * nx];
+                }
+            }
+            if (kAdj) {
+                // warp-shuffle reduction of the row moments
+#pragma unroll
+                for (int lx = 0; lx < kNPow; lx++) {
+                    double v = acc[lx];
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    acc[lx] = v;
+                }
+                if (lane == 0)
+                    for (int lx = 0; lx < L; lx++) Cx[row * L + lx] = acc[lx];
+            }
+        }
+        __syncthreads();
+        if (kAdj) {
+            // Cxy[ly][lx] = sum_rows Cx[row][lx] Y[ly][jg];  C[lz][ly][lx] += Cxy * Z[lz]
+            for (int t = tid; t < L * L; t += nthr) {
+                const int lx = t % L, ly = t / L;
+                if (lx + ly > lp) continue;
+                double s = 0.0;
+                for (int row = 0; row < nrows; row++)
+                    if (rows[2 * row + 1] >= 0) s += Cx[row * L + lx] * Yt[ly * ny + (jgmin + row - g.lb[1])];
+                for (int lz = 0; lz <= lp - lx - ly; lz++) C[(lz * L + ly) * L + lx] += s * Zk[lz * nz];
+            }
+            __syncthreads();
+        }
+    }
+    if (kAdj) {
+        for (int t = tid; t < L * L * L; t += nthr) {
+            const int lx = t % L, ly = (t / L) % L, lz = t / (L * L);
+            if (lx + ly + lz <= lp) mom[g.coef_off + pidx(lp, lz, ly, lx)] = C[t];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// general cell, one CTA per pair: rows of the index box, i-range from the
+// quadratic |i h0 + v|^2 <= r^2 (grid_base_ref_c.cc:781-807)
+GPW_HD bool general_row(const double dh[3][3], const double gp[3], double dj, double dk,
+                        double radius, int &ismin, int &ismax) {
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = 0; i < 3; i++) {
+        const double pointk = rmul(dh[2][i], dk);
+        const double pointj = radd(pointk, rmul(dh[1][i], dj));
+        const double v = rsub(pointj, rmul(gp[0], dh[0][i]));
+        a = radd(a, rmul(dh[0][i], dh[0][i]));
+        b = radd(b, rmul(rmul(2.0, v), dh[0][i]));
+        c = radd(c, rmul(v, v));
+    }
+    double d = rsub(rmul(b, b), rmul(rmul(4.0, a), rsub(c, rmul(radius, radius))));
+    if (d < 0.0) return false;
+    d = rsqrt_rn(d);
+    const double a2 = rmul(2.0, a);
+    ismin = (int)ceil(rdiv(rsub(-b, d), a2));
+    ismax = (int)floor(rdiv(radd(-b, d), a2));
+    return true;
+}
+
+int smem_general_fp64(const PairGeom &g) {
+    const int L = g.lp + 1;
+    const int ny = g.hi[1] - g.cc[1] + 1;
+    return 8 * (L * L * L + L * L + ny * L) + 12 * ny;
+}
+
+template <bool kAdj>
+__global__ void __launch_bounds__(256)
+k_general_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__restrict__ levels,
+               const double *__restrict__ coef, double *__restrict__ mom, GridPtrs grids,
+               int *status) {
+    extern __shared__ double sm[];
+    const PairGeom g = geoms[first + blockIdx.x];
+    const LevelDev &lv = levels[g.level];
+    double *__restrict__ grid = grids.p[g.level];
+    const int lp = g.lp, L = lp + 1;
+    const int ny = g.hi[1] - g.cc[1] + 1;
+    double *Q = sm;              // [k][j][i] dense
+    double *Qjk = Q + L * L * L; // [j][i]
+    double *Qj = Qjk + L * L;    // [row][i]
+    int *rows = (int *)(Qj + ny * L);  // ismin, ismax, jidx
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+    for (int t = tid; t < L * L * L; t += nthr) {
+        const int i = t % L, j = (t / L) % L, k = t / (L * L);
+        Q[t] = (!kAdj && i + j + k <= lp) ? coef[g.coef_off + pidx(lp, k, j, i)] : 0.0;
+    }
+    __syncthreads();
+    int off[3];
+    for (int d = 0; d < 3; d++) off[d] = imod(g.cc[d] + lv.lb_grid[d], lv.npts[d]);
+    for (int kk = g.cc[2]; kk <= g.hi[2]; kk++) {
+        const double dk = rsub((double)kk, g.off[2]);
+        const int kidx = lv.periodic[2] ? imod(kk, lv.npts[2]) : kk - g.cc[2] + off[2];
+        if (kidx < 0 || kidx >= lv.ngrid[2]) {
+            if (tid == 0) atomicOr(status, kStatOutOfWindow);
+            continue;
+        }
+        if (!kAdj) {
+            for (int t = tid; t < L * L; t += nthr) {
+                const int i = t % L, j = t / L;
+                double s = 0.0, p = 1.0;
+                for (int k = 0; k <= lp - i - j; k++) {
+                    s += Q[(k * L + j) * L + i] * p;
+                    p *= dk;
+                }
+                Qjk[t] = s;
+            }
+            __syncthreads();
+        }
+        for (int t = tid; t < ny * L; t += nthr) {
+            const int row = t / L, i = t % L;
+            const int jj = g.cc[1] + row;
+            const double dj = rsub((double)jj, g.off[1]);
+            if (!kAdj) {
+                double s = 0.0, p = 1.0;
+                for (int j = 0; j <= lp - i; j++) {
+                    s += Qjk[j * L + i] * p;
+                    p *= dj;
+                }
+                Qj[t] = s;
+            }
+            if (i == 0) {
+                int ismin = 0, ismax = -1;
+                if (!general_row(lv.dh, g.off, dj, dk, g.radius, ismin, ismax)) { ismin = 0; ismax = -1; }
+                rows[3 * row] = ismin;
+                rows[3 * row + 1] = ismax;
+                rows[3 * row + 2] = lv.periodic[1] ? imod(jj, lv.npts[1]) : jj - g.cc[1] + off[1];
+            }
+        }
+        __syncthreads();
+        for (int row = warp; row < ny; row += nwarp) {
+            const int ismin = rows[3 * row], ismax = rows[3 * row + 1], jidx = rows[3 * row + 2];
+            if (ismax < ismin) continue;
+            if (jidx < 0 || jidx >= lv.ngrid[1]) {
+                if (lane == 0) atomicOr(status, kStatOutOfWindow);
+                continue;
+            }
+            const double dj = (double)(g.cc[1] + row) - g.off[1];
+            const int64_t rowbase = ((int64_t)kidx * lv.ngrid[1] + jidx) * lv.ngrid[0];
+            double acc[kNPow];
+#pragma unroll
+            for (int n = 0; n < kNPow; n++) acc[n] = 0.0;
+            for (int ii = ismin + lane; ii <= ismax; ii += 32) {
+                const int iidx = lv.periodic[0] ? imod(ii, lv.npts[0]) : ii - g.cc[0] + off[0];
+                if (iidx < 0 || iidx >= lv.ngrid[0]) {
+                    atomicOr(status, kStatOutOfWindow);
+                    continue;
+                }
+                const double di = (double)ii - g.off[0];
+                double r2 = 0.0;
+                for (int c = 0; c < 3; c++) {
+                    const double rc = di * lv.dh[0][c] + dj * lv.dh[1][c] + dk * lv.dh[2][c];
+                    r2 += rc * rc;
+                }
+                const double e = exp(-g.zetp * r2);
+                if (!kAdj) {
+                    double s = 0.0, p = 1.0;
+                    for (int n = 0; n < L; n++) {
+                        s += Qj[row * L + n] * p;
+                        p *= di;
+                    }
+                    atomicAdd(grid + rowbase + iidx, s * e);
+                } else {
+                    const double ve = grid[rowbase + iidx] * e;
+                    double p = 1.0;
+#pragma unroll
+                    for (int n = 0; n < kNPow; n++) {
+                        if (n < L) acc[n] += ve * p;
+                        p *= di;
+                    }
+                }
+            }
+            if (kAdj) {
+#pragma unroll
+                for (int n = 0; n < kNPow; n++) {
+                    double v = acc[n];
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    acc[n] = v;
+                }
+                if (lane == 0)
+                    for (int n = 0; n < L; n++) Qj[row * L + n] = acc[n];
+            }
+        }
+        __syncthreads();
+        if (kAdj) {
+            // Qjk[j][i] = sum_rows Qj[row][i] dj^j;  Q[k][j][i] += Qjk[j][i] dk^k
+            for (int t = tid; t < L * L; t += nthr) {
+                const int i = t % L, j = t / L;
+                if (i + j > lp) continue;
+                double s = 0.0;
+                for (int row = 0; row < ny; row++) {
+                    if (rows[3 * row + 1] < rows[3 * row]) continue;
+                    const double dj = (double)(g.cc[1] + row) - g.off[1];
+                    double p = 1.0;
+                    for (int e = 0; e < j; e++) p *= dj;
+                    s += Qj[row * L + i] * p;
+                }
+                double p = 1.0;
+                for (int k = 0; k <= lp - i - j; k++) {
+                    Q[(k * L + j) * L + i] += s * p;
+                    p *= dk;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (kAdj) {
+        for (int t = tid; t < L * L * L; t += nthr) {
+            const int i = t % L, j = (t / L) % L, k = t / (L * L);
+            if (i + j + k <= lp) mom[g.coef_off + pidx(lp, k, j, i)] = Q[t];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+static cudaError_t set_smem(const void *fn, int bytes) {
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t launch_prep(const TaskSet &ts, const double *d_pab, cudaStream_t s) {
+    if (ts.ntasks == 0) return cudaSuccess;
+    const int smem = smem_prep(ts.max_A, ts.max_B);
+    cudaError_t e = set_smem((const void *)k_prep, smem);
+    if (e != cudaSuccess) return e;
+    ts.n_kernels++;
+    k_prep<<<(unsigned)ts.ntasks, 128, smem, s>>>(ts.d_geom, ts.plan->d_levels, ts.plan->d_tmat,
+                                                  ts.tau, d_pab, ts.d_coef);
+    return cudaGetLastError();
+}
+
+static cudaError_t launch_fp64(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s) {
+    for (const Chunk &c : ts.chunks) {
+        if (c.count == 0) continue;
+        const void *fn;
+        if (c.kind == 0)
+            fn = adj ? (const void *)k_ortho_fp64<true> : (const void *)k_ortho_fp64<false>;
+        else
+            fn = adj ? (const void *)k_general_fp64<true> : (const void *)k_general_fp64<false>;
+        cudaError_t e = set_smem(fn, c.smem_bytes);
+        if (e != cudaSuccess) return e;
+        ProfScope prof(ts, s);
+        if (c.kind == 0) {
+            if (adj)
+                k_ortho_fp64<true><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
+                                                                     ts.d_table, ts.d_coef, ts.d_mom, g,
+                                                                     ts.d_status);
+            else
+                k_ortho_fp64<false><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
+                                                                      ts.d_table, ts.d_coef, ts.d_mom, g,
+                                                                      ts.d_status);
+        } else {
+            if (adj)
+                k_general_fp64<true><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
+                                                                       ts.d_coef, ts.d_mom, g, ts.d_status);
+            else
+                k_general_fp64<false><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
+                                                                        ts.d_coef, ts.d_mom, g, ts.d_status);
+        }
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
+    return launch_fp64(ts, g, false, s);
+}
+
+cudaError_t launch_integrate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
+    return launch_fp64(ts, g, true, s);
+}
+
+cudaError_t launch_backtransform(const TaskSet &ts, const double *d_mom, double *d_hab,
+                                 cudaStream_t s) {
+    if (ts.ntasks == 0) return cudaSuccess;
+    const int smem = smem_prep(ts.max_A, ts.max_B);
+    cudaError_t e = set_smem((const void *)k_backtransform, smem);
+    if (e != cudaSuccess) return e;
+    ts.n_kernels++;
+    k_backtransform<<<(unsigned)ts.ntasks, 128, smem, s>>>(ts.d_geom, ts.plan->d_levels,
+                                                           ts.plan->d_tmat, ts.tau, d_mom, d_hab);
+    return cudaGetLastError();
+}
+
+}  // namespace gpw

@@ -1,0 +1,108 @@
+// Internal host-side interfaces between the C ABI and the kernel files.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gpw_common.cuh"
+
+namespace gpw {
+
+struct GridPtrs {
+    double *p[GPW_MAX_LEVELS];
+};
+
+// A contiguous run of sorted tasks launched together (same kind, similar size).
+struct Chunk {
+    int first, count;
+    int smem_bytes;
+    int kind;  // 0 ortho, 1 general
+};
+
+struct Plan {
+    int device = 0;
+    int nlevels = 0;
+    LevelDev lv[GPW_MAX_LEVELS];
+    LevelDev *d_levels = nullptr;
+    double *d_tmat = nullptr;  // lattice transforms of general levels
+    std::vector<double> h_tmat;
+};
+
+struct MixedState;  // tiled path, gpw_mixed.cu
+
+struct TaskSet {
+    Plan *plan = nullptr;
+    int tau = 0;
+    int64_t ntasks = 0;
+    int64_t pab_extent = 0;
+    int max_lp = 0;
+    int max_A = 0, max_B = 0;
+    std::vector<PairGeom> h_geom;  // sorted
+    PairGeom *d_geom = nullptr;
+    int *d_table = nullptr;        // random-access cube lists (explicit tables)
+    double *d_coef = nullptr;      // packed coefficients, per call
+    double *d_mom = nullptr;       // packed moments (integrate), per call
+    int64_t coef_len = 0;
+    int *d_status = nullptr;
+    std::vector<Chunk> chunks;     // FP64 launches
+    MixedState *mixed = nullptr;
+    // profiling (gpw_taskset_profile / gpw_taskset_stats)
+    bool profile = false;
+    mutable std::vector<cudaEvent_t> ev_pool;
+    mutable size_t ev_used = 0;
+    mutable int64_t n_kernels = 0;
+    mutable int64_t n_contract = 0;
+};
+
+// Brackets a contraction launch with events when profiling is on.
+struct ProfScope {
+    const TaskSet &ts;
+    cudaStream_t s;
+    ProfScope(const TaskSet &t, cudaStream_t st) : ts(t), s(st) {
+        ts.n_kernels++;
+        ts.n_contract++;
+        if (ts.profile) record();
+    }
+    ~ProfScope() {
+        if (ts.profile) record();
+    }
+    void record() {
+        if (ts.ev_used == ts.ev_pool.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            ts.ev_pool.push_back(e);
+        }
+        cudaEventRecord(ts.ev_pool[ts.ev_used++], s);
+    }
+};
+
+// gpw_fp64.cu
+cudaError_t launch_prep(const TaskSet &ts, const double *d_pab, cudaStream_t s);
+cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
+cudaError_t launch_integrate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
+cudaError_t launch_backtransform(const TaskSet &ts, const double *d_mom, double *d_hab,
+                                 cudaStream_t s);
+int smem_ortho_fp64(const PairGeom &g);
+int smem_general_fp64(const PairGeom &g);
+int smem_prep(int A, int B);
+
+// gpw_core.cu
+cudaError_t launch_collocate_core(const int length[3], int L, const double *co, const double *pol,
+                                  int ld, double *out, cudaStream_t s);
+cudaError_t launch_integrate_core(const int length[3], int L, const double *pol, int ld,
+                                  const double *V, double *co, cudaStream_t s);
+
+// gpw_mixed.cu
+int mixed_build(TaskSet &ts, std::string &err);
+void mixed_free(TaskSet &ts);
+cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
+cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
+
+// gpw_backward.cu
+cudaError_t launch_backward(const TaskSet &ts, const double *d_pab, const GridPtrs &g,
+                            double *d_hab, double *d_dra, double *d_drb, double *d_dza,
+                            double *d_dzb, cudaStream_t s);
+
+}  // namespace gpw
