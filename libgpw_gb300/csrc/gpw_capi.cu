@@ -495,7 +495,9 @@ int gpw_collocate(gpw_taskset *ts, int precision, const double *d_pab, double *c
     if (precision == GPW_PREC_FP64) {
         GPW_CUDA(launch_collocate_fp64(*ts, g, s));
     } else if (precision == GPW_PREC_MIXED) {
-        GPW_CUDA(launch_collocate_mixed(*ts, g, s));
+        cudaError_t e = launch_collocate_mixed(*ts, g, s);
+        if (e == cudaErrorNotSupported) return fail(GPW_ERR_UNSUPPORTED, "gpw_collocate: mixed path not built");
+        if (e != cudaSuccess) return cuda_fail(e, "gpw_collocate (mixed)");
     } else {
         return fail(GPW_ERR_INVALID_ARG, "gpw_collocate: unknown precision");
     }
@@ -511,7 +513,9 @@ int gpw_integrate(gpw_taskset *ts, int precision, double *const *d_grids, double
     if (precision == GPW_PREC_FP64) {
         GPW_CUDA(launch_integrate_fp64(*ts, g, s));
     } else if (precision == GPW_PREC_MIXED) {
-        GPW_CUDA(launch_integrate_mixed(*ts, g, s));
+        cudaError_t e = launch_integrate_mixed(*ts, g, s);
+        if (e == cudaErrorNotSupported) return fail(GPW_ERR_UNSUPPORTED, "gpw_integrate: mixed path not built");
+        if (e != cudaSuccess) return cuda_fail(e, "gpw_integrate (mixed)");
     } else {
         return fail(GPW_ERR_INVALID_ARG, "gpw_integrate: unknown precision");
     }
@@ -545,6 +549,8 @@ int gpw_taskset_check(gpw_taskset *ts, void *stream) {
     if (h & kStatOutOfWindow) return fail(GPW_ERR_OUT_OF_WINDOW, "a cube left the local grid window");
     if (h & kStatTimeout) return fail(GPW_ERR_TIMEOUT, "a bounded device wait gave up");
     if (h & kStatBadTable) return fail(GPW_ERR_INVALID_ARG, "a cube list was inconsistent on the device");
+    if (h & kStatTooManyImages)
+        return fail(GPW_ERR_UNSUPPORTED, "a cube spans more periodic images than the tiled path handles");
     return GPW_SUCCESS;
 }
 

@@ -162,6 +162,7 @@ enum : int {
     kStatOutOfWindow = 1,
     kStatTimeout = 2,
     kStatBadTable = 4,
+    kStatTooManyImages = 8,
 };
 
 }  // namespace gpw

@@ -481,9 +481,9 @@ cudaError_t launch_prep(const TaskSet &ts, const double *d_pab, cudaStream_t s) 
     return cudaGetLastError();
 }
 
-static cudaError_t launch_fp64(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s) {
+cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, cudaStream_t s) {
     for (const Chunk &c : ts.chunks) {
-        if (c.count == 0) continue;
+        if (c.count == 0 || (kind >= 0 && c.kind != kind)) continue;
         const void *fn;
         if (c.kind == 0)
             fn = adj ? (const void *)k_ortho_fp64<true> : (const void *)k_ortho_fp64<false>;
@@ -516,11 +516,11 @@ static cudaError_t launch_fp64(const TaskSet &ts, const GridPtrs &g, bool adj, c
 }
 
 cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
-    return launch_fp64(ts, g, false, s);
+    return launch_fp64_kind(ts, g, false, -1, s);
 }
 
 cudaError_t launch_integrate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
-    return launch_fp64(ts, g, true, s);
+    return launch_fp64_kind(ts, g, true, -1, s);
 }
 
 cudaError_t launch_backtransform(const TaskSet &ts, const double *d_mom, double *d_hab,

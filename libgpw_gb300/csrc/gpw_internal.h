@@ -82,6 +82,8 @@ struct ProfScope {
 cudaError_t launch_prep(const TaskSet &ts, const double *d_pab, cudaStream_t s);
 cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 cudaError_t launch_integrate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
+// kind: 0 orthorhombic chunks, 1 general-cell chunks, -1 all
+cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, cudaStream_t s);
 cudaError_t launch_backtransform(const TaskSet &ts, const double *d_mom, double *d_hab,
                                  cudaStream_t s);
 int smem_ortho_fp64(const PairGeom &g);

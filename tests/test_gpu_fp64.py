@@ -56,9 +56,9 @@ def test_task_files_explicit_cube(name):
 def test_dropin_entry(name):
     """gpw_collocate_pgf_product_rspace: same arguments as the reference, accumulates."""
     d = load_task(name)
-    grid = np.ones((d["ngrid"][2], d["ngrid"][1], d["ngrid"][0]))
+    grid = np.ascontiguousarray(d["grid_ref"]).copy()  # accumulates onto what is there
     capi.collocate_pgf_product_rspace(d, grid)
-    assert rel_l2(grid - 1.0, d["grid_ref"]) <= ref_tol(name)
+    assert rel_l2(grid, 2.0 * d["grid_ref"]) <= ref_tol(name)
 
 
 def test_adjoint_identity_gpu():
