@@ -176,6 +176,14 @@ int gpw_taskset_profile(gpw_taskset *ts, int enable);
 int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
                       int64_t *contraction_launches, int64_t *kernel_launches);
 
+/*
+ * Tensor-core self test on the current device: one fp16 MMA with FP32
+ * accumulation (M=128, N=32, K=16) on integer-valued operands in the operand
+ * layout the mixed path uses, compared exactly with the integer products.
+ * *mismatches receives the number of wrong elements (0 when the path works).
+ */
+int gpw_selftest_tensorcore(int64_t *mismatches);
+
 /* Host-buffer convenience calls (copies inside, synchronous) ------------- */
 int gpw_collocate_host(gpw_taskset *ts, int precision, const double *h_pab,
                        double *const *h_grids);

@@ -65,6 +65,7 @@ def lib():
                                                                                 i32, i32, vp, vp], i32),
         "gpw_taskset_profile": ([vp, i32], i32),
         "gpw_taskset_stats": ([vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)], i32),
+        "gpw_selftest_tensorcore": ([C.POINTER(i64)], i32),
         "gpw_collocate_core": ([vp, i32, vp, vp, i32, vp, vp], i32),
         "gpw_integrate_core": ([vp, i32, vp, i32, vp, vp, vp], i32),
     }
@@ -207,6 +208,13 @@ class TaskSet:
         gr = [np.ascontiguousarray(g, dtype=np.float64) for g in grids]
         ptrs = (C.c_void_p * len(gr))(*[g.ctypes.data for g in gr])
         check(lib().gpw_integrate_host(self.handle, PREC[precision], ptrs, hab.ctypes.data), "gpw_integrate_host")
+
+
+def selftest_tensorcore() -> int:
+    """Runs gpw_selftest_tensorcore; returns the number of wrong MMA elements."""
+    n = C.c_int64(-1)
+    check(lib().gpw_selftest_tensorcore(C.byref(n)), "gpw_selftest_tensorcore")
+    return n.value
 
 
 def collocate_pgf_product_rspace(t: dict, grid: np.ndarray) -> None:

@@ -685,6 +685,15 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
     return st;
 }
 
+int gpw_selftest_tensorcore(int64_t *mismatches) {
+    if (!mismatches) return fail(GPW_ERR_INVALID_ARG, "gpw_selftest_tensorcore: null");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GPW_ERR_NO_DEVICE, "no CUDA device");
+    std::string err;
+    const int st = tc_selftest(mismatches, err);
+    return st ? fail(st, err) : GPW_SUCCESS;
+}
+
 int gpw_collocate_core(const int length[3], int L, const double *d_co, const double *d_pol, int ld_pol,
                        double *d_out, void *stream) {
     if (!length || L < 1 || L > 16 || !d_co || !d_pol || !d_out || ld_pol < std::max({length[0], length[1], length[2]}))

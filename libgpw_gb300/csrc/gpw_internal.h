@@ -102,6 +102,9 @@ void mixed_free(TaskSet &ts);
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 
+// gpw_selftest.cu
+int tc_selftest(int64_t *mismatches, std::string &err);
+
 // gpw_backward.cu
 cudaError_t launch_backward(const TaskSet &ts, const double *d_pab, const GridPtrs &g,
                             double *d_hab, double *d_dra, double *d_drb, double *d_dza,

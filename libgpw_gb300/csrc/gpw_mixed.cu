@@ -32,6 +32,7 @@
 #include "gpw_coef.cuh"
 #include "gpw_ff.cuh"
 #include "gpw_internal.h"
+#include "gpw_tc.cuh"
 
 namespace gpw {
 
@@ -60,7 +61,8 @@ struct MixedState {
     float2 *d_coef_ff = nullptr;
     int *d_queue = nullptr;      // [0]: collocate, [1]: integrate
     int northo = 0;              // ortho tasks come first in sorted order
-    int grid_ctas = 0;
+    int grid_ctas = 0;    // collocate
+    int grid_ctas_i = 0;  // integrate
 };
 
 // ---------------------------------------------------------------------------
@@ -77,6 +79,7 @@ struct TPair {
     int64_t coef_off, table_off;
     int o[3];           // cube offset of the tile origin (current image)
     int gx0, gx1;       // tile-local x range inside the cube box
+    int sx;             // x-variable rescale exponent of the current image
 };
 
 // ---------------------------------------------------------------------------
@@ -195,26 +198,42 @@ struct MixedArgs {
     int ntiles;
 };
 
-struct TileSmem {
+// shared state of both tiled kernels
+struct TileCommon {
     TPair p;
     float2 coef[NCOEF_MAX];
     ff X[KP][TX];
     ff Y[KP][TY];
     ff Z[KP][TZ];
     ff Cxy[TZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
-    __half A[NSL][MROWS * KP];
-    __half B[NSL][TX * KP];
-    int fx[TX];             // column exponents (collocate: per x; integrate: per alpha)
-    ff S[MROWS][KP];        // integrate: per-row moments
     int tile;
-    int img[3][kMaxImages];  // image offsets per axis
+    int img[3][kMaxImages];
     int nimg[3];
+    uint64_t mbar;
+    uint32_t tmem;
+    int abort;
+};
+
+struct alignas(128) SmemColl {
+    __half A[NSL][MROWS * KP];  // Cx slices, M=128 x K=16
+    __half B[NSL][TX * KP];     // X' slices, N=32 x K=16
+    int fx[TX];
+    TileCommon c;
+};
+
+struct alignas(128) SmemInt {
+    __half A[2][NSL][MROWS * KP];  // masked V slices, K halves x in [0,16) and [16,32)
+    __half B[2][NSL][KP * KP];     // X' slices, N=16 (alpha) x K=16 per half
+    __half Vs[NSL][MROWS][TX];     // this tile's V slices, unmasked
+    ff S[MROWS][KP];
+    int gexp[KP];
+    TileCommon c;
 };
 
 // pair index of (b, a), b + a <= lp, rows of constant b
 __device__ __forceinline__ int pair_index(int L, int b, int a) { return b * L - (b * (b - 1)) / 2 + a; }
 
-__device__ void load_pair(TileSmem &sm, const MixedArgs &A, const LevelDev &lv, int task) {
+__device__ void load_pair(TileCommon &sm, const MixedArgs &A, const LevelDev &lv, int task) {
     if (threadIdx.x == 0) {
         const PairGeom &g = A.geoms[task];
         TPair &p = sm.p;
@@ -252,7 +271,6 @@ __device__ void axis_images(const LevelDev &lv, int d, int tt, int T, const TPai
     const int ext = min(T, N - tt * T);
     if (lv.periodic[d]) {
         const int np = lv.npts[d];
-        // o = k*np + tt*T - cc, need [o, o+ext-1] to meet [lb, hi]
         const int base = tt * T - p.cc[d];
         const int num = p.lb[d] - base - ext + 1;
         const int kmin = (num >= 0 ? num / np : -((-num + np - 1) / np)) - 1;
@@ -274,10 +292,28 @@ __device__ void axis_images(const LevelDev &lv, int d, int tt, int T, const TPai
     }
 }
 
-// tables over the tile's range on one axis: tab[k][i] = t^k exp(-zetp t^2), t = g h - off,
-// g = o + i; zero outside [lb, hi] and outside the valid tile extent.
+// Per image: tile origin in cube offsets, the x range inside the cube box, and
+// the power-of-two rescale of the x variable t -> t / 2^sx (|t / 2^sx| < 1 on
+// the tile), which balances the columns t^k exp(-zetp t^2) of stage 3.  The
+// factor 2^(k sx) goes to the row coefficients, so the product is unchanged.
+__device__ __forceinline__ void set_image(TPair &p, int ox, int oy, int oz, int ext_x) {
+    p.o[0] = ox;
+    p.o[1] = oy;
+    p.o[2] = oz;
+    p.gx0 = max(0, p.lb[0] - ox);
+    p.gx1 = min(ext_x - 1, p.hi[0] - ox);
+    const float hx = p.h[0].hi, of = p.off[0].hi;
+    const float t0 = fabsf((float)(ox + p.gx0) * hx - of), t1 = fabsf((float)(ox + p.gx1) * hx - of);
+    int e = 0;
+    const float m = fmaxf(t0, t1);
+    if (m >= 1.0f) frexpf(m, &e);
+    p.sx = min(e, 30);
+}
+
+// tab[k][i] = (t/2^sx)^k exp(-zetp t^2), t = g h - off, g = o + i; zero outside the
+// cube box and outside the valid tile extent.
 __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool inside, ff *col, int stride,
-                                            int L) {
+                                            int L, int sx) {
     if (!inside) {
         for (int k = 0; k < KP; k++) col[k * stride] = ff{0.0f, 0.0f};
         return;
@@ -285,59 +321,86 @@ __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool i
     const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
     const ff a = ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo});
     ff e = ff_exp(a);
+    const ff ts = {ldexpf(t.hi, -sx), ldexpf(t.lo, -sx)};
     for (int k = 0; k < KP; k++) {
         col[k * stride] = k < L ? e : ff{0.0f, 0.0f};
-        if (k + 1 < L) e = ff_mul(e, t);
+        if (k + 1 < L) e = ff_mul(e, ts);
     }
 }
 
-__device__ void build_tables(TileSmem &sm, const LevelDev &lv, const TileDesc &td) {
+__device__ void build_tables(TileCommon &sm, const LevelDev &lv, const TileDesc &td) {
     const TPair &p = sm.p;
     const int tid = threadIdx.x;
-    // 32 x + 8 y + 16 z = 56 entries
     if (tid < TX) {
         const int g = p.o[0] + tid;
-        const bool in = tid < min(TX, lv.ngrid[0] - td.t[0] * TX) && g >= p.lb[0] && g <= p.hi[0];
-        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L);
+        const bool in = tid >= p.gx0 && tid <= p.gx1;
+        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L, p.sx);
     } else if (tid < TX + TY) {
         const int i = tid - TX, g = p.o[1] + i;
         const bool in = i < min(TY, lv.ngrid[1] - td.t[1] * TY) && g >= p.lb[1] && g <= p.hi[1];
-        table_entry(p, 1, g, in, &sm.Y[0][i], TY, p.L);
+        table_entry(p, 1, g, in, &sm.Y[0][i], TY, p.L, 0);
     } else if (tid < TX + TY + TZ) {
         const int i = tid - TX - TY, g = p.o[2] + i;
         const bool in = i < min(TZ, lv.ngrid[2] - td.t[2] * TZ) && g >= p.lb[2] && g <= p.hi[2];
-        table_entry(p, 2, g, in, &sm.Z[0][i], TZ, p.L);
+        table_entry(p, 2, g, in, &sm.Z[0][i], TZ, p.L, 0);
     }
 }
 
-// ---------------------------------------------------------------------------
-// SIMT stage 3 on the slices: rows m, columns c, K = 16.
-__device__ __forceinline__ void slice_dot(const __half *A0, const __half *A1, const __half *A2, const __half *B0,
-                                          const __half *B1, const __half *B2, int m, int c, float &d2, float &d3,
-                                          float &d4) {
-    d2 = d3 = d4 = 0.0f;
-#pragma unroll
-    for (int k = 0; k < KP; k++) {
-        const int oa = umma_off(m, k) >> 1, ob = umma_off(c, k) >> 1;
-        const float a0 = __half2float(A0[oa]), a1 = __half2float(A1[oa]), a2 = __half2float(A2[oa]);
-        const float b0 = __half2float(B0[ob]), b1 = __half2float(B1[ob]), b2 = __half2float(B2[ob]);
-        d2 = __fmaf_rn(a0, b0, d2);
-        d3 = __fmaf_rn(a0, b1, __fmaf_rn(a1, b0, d3));
-        d4 = __fmaf_rn(a0, b2, __fmaf_rn(a1, b1, __fmaf_rn(a2, b0, d4)));
+__device__ __forceinline__ ff ff_ldexp(ff v, int e) { return {ldexpf(v.hi, e), ldexpf(v.lo, e)}; }
+
+// TMEM set-up shared by both kernels: warp 0 allocates, thread 0 inits the mbarrier
+__device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&c.mbar, 1);
+        tc::fence_mbar_init();
+        c.abort = 0;
     }
+    if (threadIdx.x < 32) {
+        tc::tmem_alloc(&c.tmem, ncols);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
 }
+
+__device__ __forceinline__ void tc_teardown(TileCommon &c, uint32_t ncols, uint32_t phase) {
+    if (c.abort) tc::mbar_wait_bounded(&c.mbar, phase, 1u << 22);  // let an MMA in flight finish
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_dealloc(c.tmem, ncols);
+}
+
+// waits for the MMAs of this round; false (and abort flagged) on timeout
+__device__ __forceinline__ bool tc_wait(TileCommon &c, uint32_t phase, int *status) {
+    if (!tc::mbar_wait_bounded(&c.mbar, phase, 1u << 24)) {
+        atomicOr(status, kStatTimeout);
+        c.abort = 1;
+    }
+    __syncthreads();
+    tc::fence_after_sync();
+    return !c.abort;
+}
+
+constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    TileSmem &sm = *reinterpret_cast<TileSmem *>(smraw);
-    const int tid = threadIdx.x;
+    SmemColl &sm = *reinterpret_cast<SmemColl *>(smraw);
+    TileCommon &cm = sm.c;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const int m = tid, z = m / TY, y = m % TY;
+    constexpr uint32_t kCols = 128;  // D2, D3, D4: 32 columns each
+    tc_setup(cm, kCols);
+    const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t idesc = tc::idesc_f16_f32(MROWS, TX);
+    uint32_t phase = 0;
     for (;;) {
-        if (tid == 0) sm.tile = atomicAdd(A.queue, 1);
+        if (tid == 0) cm.tile = atomicAdd(A.queue, 1);
         __syncthreads();
-        const int tile = sm.tile;
-        if (tile >= A.ntiles) break;
+        const int tile = cm.tile;
+        if (tile >= A.ntiles || cm.abort) break;
         const TileDesc td = A.tiles[tile];
         const LevelDev &lv = A.levels[td.level];
         float acc_hi[TX], acc_lo[TX];
@@ -345,27 +408,23 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
         for (int x = 0; x < TX; x++) acc_hi[x] = acc_lo[x] = 0.0f;
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
-        for (int64_t it = A.start[tile]; it < A.start[tile + 1]; it++) {
-            const int task = A.items[it];
-            load_pair(sm, A, lv, task);
+        for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
+            load_pair(cm, A, lv, A.items[it]);
             if (tid < 3) {
                 const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
-                axis_images(lv, tid, td.t[tid], T, sm.p, sm.img[tid], sm.nimg[tid], A.status);
+                axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
             }
             __syncthreads();
-            const int L = sm.p.L, lp = sm.p.lp;
-            for (int iz = 0; iz < sm.nimg[2]; iz++)
-            for (int iy = 0; iy < sm.nimg[1]; iy++)
-            for (int ix = 0; ix < sm.nimg[0]; ix++) {
+            const int L = cm.p.L, lp = cm.p.lp;
+            const int nimg = cm.nimg[0] * cm.nimg[1] * cm.nimg[2];
+            for (int im = 0; im < nimg && !cm.abort; im++) {
                 if (tid == 0) {
-                    sm.p.o[0] = sm.img[0][ix];
-                    sm.p.o[1] = sm.img[1][iy];
-                    sm.p.o[2] = sm.img[2][iz];
-                    sm.p.gx0 = max(0, sm.p.lb[0] - sm.p.o[0]);
-                    sm.p.gx1 = min(ext_x - 1, sm.p.hi[0] - sm.p.o[0]);
+                    const int ix = im % cm.nimg[0], iy = (im / cm.nimg[0]) % cm.nimg[1], iz = im / (cm.nimg[0] * cm.nimg[1]);
+                    set_image(cm.p, cm.img[0][ix], cm.img[1][iy], cm.img[2][iz], ext_x);
                 }
                 __syncthreads();
-                build_tables(sm, lv, td);
+                if (cm.p.gx0 > cm.p.gx1) continue;  // uniform: no x overlap
+                build_tables(cm, lv, td);
                 __syncthreads();
                 // stage 1: Cxy[z][(b,a)] = sum_g c[g][b][a] Z[g][z]
                 const int npair = (L * (L + 1)) / 2;
@@ -376,32 +435,32 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                     const int a = q;
                     ff s = {0.0f, 0.0f};
                     for (int g = 0; g <= lp - a - b; g++) {
-                        const float2 c = sm.coef[pidx(lp, g, b, a)];
-                        s = ff_fma(ff{c.x, c.y}, sm.Z[g][zz], s);
+                        const float2 c = cm.coef[pidx(lp, g, b, a)];
+                        s = ff_fma(ff{c.x, c.y}, cm.Z[g][zz], s);
                     }
-                    sm.Cxy[zz][pair_index(L, b, a)] = s;
+                    cm.Cxy[zz][pair_index(L, b, a)] = s;
                 }
                 // B slices: column x over alpha
                 if (tid < TX) {
                     ff col[KP];
 #pragma unroll
-                    for (int k = 0; k < KP; k++) col[k] = sm.X[k][tid];
+                    for (int k = 0; k < KP; k++) col[k] = cm.X[k][tid];
                     const int e = slice_exponent(col, KP);
                     sm.fx[tid] = e;
 #pragma unroll
                     for (int k = 0; k < KP; k++) {
-                        float s[3];
-                        slice_value(col[k], e, s);
+                        float sl[3];
+                        slice_value(col[k], e, sl);
                         const int o = umma_off(tid, k) >> 1;
-                        sm.B[0][o] = __float2half_rn(s[0]);
-                        sm.B[1][o] = __float2half_rn(s[1]);
-                        sm.B[2][o] = __float2half_rn(s[2]);
+                        sm.B[0][o] = __float2half_rn(sl[0]);
+                        sm.B[1][o] = __float2half_rn(sl[1]);
+                        sm.B[2][o] = __float2half_rn(sl[2]);
                     }
                 }
                 __syncthreads();
                 // stage 2 + row culling + A slices (thread = row)
                 int x0, x1;
-                row_range(sm.p, A.table, sm.p.o[2] + z, sm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
+                row_range(cm.p, A.table, cm.p.o[2] + z, cm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
                 ff cx[KP];
 #pragma unroll
                 for (int a = 0; a < KP; a++) cx[a] = ff{0.0f, 0.0f};
@@ -410,37 +469,65 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                     for (int a = 0; a < KP; a++) {
                         if (a >= L) break;
                         ff s = {0.0f, 0.0f};
-                        for (int b = 0; b <= lp - a; b++) s = ff_fma(sm.Cxy[z][pair_index(L, b, a)], sm.Y[b][y], s);
-                        cx[a] = s;
+                        for (int b = 0; b <= lp - a; b++) s = ff_fma(cm.Cxy[z][pair_index(L, b, a)], cm.Y[b][y], s);
+                        cx[a] = ff_ldexp(s, a * cm.p.sx);
                     }
                 }
                 const int em = slice_exponent(cx, KP);
 #pragma unroll
                 for (int k = 0; k < KP; k++) {
-                    float s[3];
-                    slice_value(cx[k], em, s);
+                    float sl[3];
+                    slice_value(cx[k], em, sl);
                     const int o = umma_off(m, k) >> 1;
-                    sm.A[0][o] = __float2half_rn(s[0]);
-                    sm.A[1][o] = __float2half_rn(s[1]);
-                    sm.A[2][o] = __float2half_rn(s[2]);
+                    sm.A[0][o] = __float2half_rn(sl[0]);
+                    sm.A[1][o] = __float2half_rn(sl[1]);
+                    sm.A[2][o] = __float2half_rn(sl[2]);
                 }
+                // stage 3 on the tensor cores: D_s = sum_{i+j=s} A_i B_j^T
+                tc::fence_async_smem();
+                tc::fence_before_sync();
                 __syncthreads();
-                // stage 3 (SIMT on the slices) and accumulation
-                if (x0 <= x1) {
+                if (tid == 0) {
+                    tc::fence_after_sync();
+                    const uint64_t a0 = tc::desc_kmajor(sm.A[0], 128, 256), a1 = tc::desc_kmajor(sm.A[1], 128, 256),
+                                   a2 = tc::desc_kmajor(sm.A[2], 128, 256);
+                    const uint64_t b0 = tc::desc_kmajor(sm.B[0], 128, 256), b1 = tc::desc_kmajor(sm.B[1], 128, 256),
+                                   b2 = tc::desc_kmajor(sm.B[2], 128, 256);
+                    const uint32_t d = cm.tmem;
+                    tc::mma_f16(d, a0, b0, idesc, 0);
+                    tc::mma_f16(d + 32, a0, b1, idesc, 0);
+                    tc::mma_f16(d + 32, a1, b0, idesc, 1);
+                    tc::mma_f16(d + 64, a0, b2, idesc, 0);
+                    tc::mma_f16(d + 64, a1, b1, idesc, 1);
+                    tc::mma_f16(d + 64, a2, b0, idesc, 1);
+                    tc::mma_commit(&cm.mbar);
+                }
+                const bool ok = tc_wait(cm, phase, A.status);
+                phase ^= 1u;
+                if (!ok) break;
 #pragma unroll
-                    for (int x = 0; x < TX; x++) {
+                for (int c = 0; c < TX / 8; c++) {
+                    uint32_t r2[8], r3[8], r4[8];
+                    tc::tmem_ld8(tbase + 8 * c, r2);
+                    tc::tmem_ld8(tbase + 32 + 8 * c, r3);
+                    tc::tmem_ld8(tbase + 64 + 8 * c, r4);
+                    tc::tmem_wait_ld24(r2, r3, r4);
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const int x = 8 * c + i;
                         if (x < x0 || x > x1) continue;
-                        float d2, d3, d4;
-                        slice_dot(sm.A[0], sm.A[1], sm.A[2], sm.B[0], sm.B[1], sm.B[2], m, x, d2, d3, d4);
-                        const ff v = combine(d2, d3, d4, em + sm.fx[x] - 2 * SLB);
+                        const ff v = combine(__uint_as_float(r2[i]), __uint_as_float(r3[i]), __uint_as_float(r4[i]),
+                                             em + sm.fx[x] - 2 * SLB);
                         const ff s = two_sum(acc_hi[x], v.hi);
                         acc_hi[x] = s.hi;
                         acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(s.lo, v.lo));
                     }
                 }
+                tc::fence_before_sync();
                 __syncthreads();
             }
         }
+        if (cm.abort) break;
         // flush: grid += tile sum (FP64)
         if (z < ext_z && y < ext_y) {
             double *grid = A.grids.p[td.level];
@@ -452,69 +539,153 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
         }
         __syncthreads();
     }
+    tc_teardown(cm, kCols, phase);
 }
 
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    TileSmem &sm = *reinterpret_cast<TileSmem *>(smraw);
-    const int tid = threadIdx.x;
+    SmemInt &sm = *reinterpret_cast<SmemInt *>(smraw);
+    TileCommon &cm = sm.c;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const int m = tid, z = m / TY, y = m % TY;
+    constexpr uint32_t kCols = 64;  // D2 (two K halves), D3, D4: 16 columns each
+    tc_setup(cm, kCols);
+    const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t idesc = tc::idesc_f16_f32(MROWS, KP);
+    uint32_t phase = 0;
     for (;;) {
-        if (tid == 0) sm.tile = atomicAdd(A.queue, 1);
+        if (tid == 0) cm.tile = atomicAdd(A.queue, 1);
         __syncthreads();
-        const int tile = sm.tile;
-        if (tile >= A.ntiles) break;
+        const int tile = cm.tile;
+        if (tile >= A.ntiles || cm.abort) break;
         const TileDesc td = A.tiles[tile];
         const LevelDev &lv = A.levels[td.level];
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
-        // V row of this thread, float-float
-        ff v[TX];
+        // this thread's V row, sliced once per tile (row exponent vm)
+        int vm;
         {
             const double *grid = A.grids.p[td.level];
             const bool ok = z < ext_z && y < ext_y;
             const int64_t row = ((int64_t)(td.t[2] * TZ + z) * lv.ngrid[1] + (td.t[1] * TY + y)) * lv.ngrid[0] +
                                 td.t[0] * TX;
+            ff v[TX];
 #pragma unroll
             for (int x = 0; x < TX; x++) v[x] = (ok && x < ext_x) ? ff_from_double(grid[row + x]) : ff{0.0f, 0.0f};
+            vm = slice_exponent(v, TX);
+#pragma unroll
+            for (int x = 0; x < TX; x++) {
+                float sl[3];
+                slice_value(v[x], vm, sl);
+                sm.Vs[0][m][x] = __float2half_rn(sl[0]);
+                sm.Vs[1][m][x] = __float2half_rn(sl[1]);
+                sm.Vs[2][m][x] = __float2half_rn(sl[2]);
+            }
         }
-        for (int64_t it = A.start[tile]; it < A.start[tile + 1]; it++) {
-            const int task = A.items[it];
-            load_pair(sm, A, lv, task);
+        for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
+            load_pair(cm, A, lv, A.items[it]);
             if (tid < 3) {
                 const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
-                axis_images(lv, tid, td.t[tid], T, sm.p, sm.img[tid], sm.nimg[tid], A.status);
+                axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
             }
             __syncthreads();
-            const int L = sm.p.L, lp = sm.p.lp;
+            const int L = cm.p.L, lp = cm.p.lp;
             const int npair = (L * (L + 1)) / 2;
-            const int64_t moff = sm.p.coef_off;
-            for (int iz = 0; iz < sm.nimg[2]; iz++)
-            for (int iy = 0; iy < sm.nimg[1]; iy++)
-            for (int ix = 0; ix < sm.nimg[0]; ix++) {
+            const int64_t moff = cm.p.coef_off;
+            const int nimg = cm.nimg[0] * cm.nimg[1] * cm.nimg[2];
+            for (int im = 0; im < nimg && !cm.abort; im++) {
                 if (tid == 0) {
-                    sm.p.o[0] = sm.img[0][ix];
-                    sm.p.o[1] = sm.img[1][iy];
-                    sm.p.o[2] = sm.img[2][iz];
-                    sm.p.gx0 = max(0, sm.p.lb[0] - sm.p.o[0]);
-                    sm.p.gx1 = min(ext_x - 1, sm.p.hi[0] - sm.p.o[0]);
+                    const int ix = im % cm.nimg[0], iy = (im / cm.nimg[0]) % cm.nimg[1], iz = im / (cm.nimg[0] * cm.nimg[1]);
+                    set_image(cm.p, cm.img[0][ix], cm.img[1][iy], cm.img[2][iz], ext_x);
                 }
                 __syncthreads();
-                build_tables(sm, lv, td);
-                __syncthreads();
-                // stage 3 transposed: S[m][a] = sum_{x in row range} V[m][x] X[a][x]  (float-float)
+                if (cm.p.gx0 > cm.p.gx1) continue;
+                build_tables(cm, lv, td);
+                // A operand: this row's V slices masked to the row's cube range
                 int x0, x1;
-                row_range(sm.p, A.table, sm.p.o[2] + z, sm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
-                for (int a = 0; a < KP; a++) {
-                    ff s = {0.0f, 0.0f};
-                    if (a < L && x0 <= x1) {
+                row_range(cm.p, A.table, cm.p.o[2] + z, cm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
 #pragma unroll
-                        for (int x = 0; x < TX; x++)
-                            if (x >= x0 && x <= x1) s = ff_fma(v[x], sm.X[a][x], s);
-                    }
-                    sm.S[m][a] = s;
+                for (int x = 0; x < TX; x++) {
+                    const bool in = x >= x0 && x <= x1;
+                    const int o = umma_off(m, x & 15) >> 1, h = x >> 4;
+                    const __half zero = __float2half_rn(0.0f);
+                    sm.A[h][0][o] = in ? sm.Vs[0][m][x] : zero;
+                    sm.A[h][1][o] = in ? sm.Vs[1][m][x] : zero;
+                    sm.A[h][2][o] = in ? sm.Vs[2][m][x] : zero;
                 }
+                __syncthreads();
+                // B operand: X' slices per alpha over x (row exponent gexp[alpha])
+                if (tid < KP) {
+                    const int a = tid;
+                    ff row[TX];
+#pragma unroll
+                    for (int x = 0; x < TX; x++) row[x] = cm.X[a][x];
+                    const int e = slice_exponent(row, TX);
+                    sm.gexp[a] = e;
+#pragma unroll
+                    for (int x = 0; x < TX; x++) {
+                        float sl[3];
+                        slice_value(row[x], e, sl);
+                        const int o = umma_off(a, x & 15) >> 1, h = x >> 4;
+                        sm.B[h][0][o] = __float2half_rn(sl[0]);
+                        sm.B[h][1][o] = __float2half_rn(sl[1]);
+                        sm.B[h][2][o] = __float2half_rn(sl[2]);
+                    }
+                }
+                tc::fence_async_smem();
+                tc::fence_before_sync();
+                __syncthreads();
+                if (tid == 0) {
+                    tc::fence_after_sync();
+                    uint64_t a_[2][3], b_[2][3];
+                    for (int h = 0; h < 2; h++)
+                        for (int s2 = 0; s2 < 3; s2++) {
+                            a_[h][s2] = tc::desc_kmajor(sm.A[h][s2], 128, 256);
+                            b_[h][s2] = tc::desc_kmajor(sm.B[h][s2], 128, 256);
+                        }
+                    const uint32_t d = cm.tmem;
+                    tc::mma_f16(d + 0, a_[0][0], b_[0][0], idesc, 0);   // D2, x in [0,16)
+                    tc::mma_f16(d + 16, a_[1][0], b_[1][0], idesc, 0);  // D2, x in [16,32)
+                    tc::mma_f16(d + 32, a_[0][0], b_[0][1], idesc, 0);  // D3
+                    tc::mma_f16(d + 32, a_[1][0], b_[1][1], idesc, 1);
+                    tc::mma_f16(d + 32, a_[0][1], b_[0][0], idesc, 1);
+                    tc::mma_f16(d + 32, a_[1][1], b_[1][0], idesc, 1);
+                    tc::mma_f16(d + 48, a_[0][0], b_[0][2], idesc, 0);  // D4
+                    tc::mma_f16(d + 48, a_[1][0], b_[1][2], idesc, 1);
+                    tc::mma_f16(d + 48, a_[0][1], b_[0][1], idesc, 1);
+                    tc::mma_f16(d + 48, a_[1][1], b_[1][1], idesc, 1);
+                    tc::mma_f16(d + 48, a_[0][2], b_[0][0], idesc, 1);
+                    tc::mma_f16(d + 48, a_[1][2], b_[1][0], idesc, 1);
+                    tc::mma_commit(&cm.mbar);
+                }
+                const bool ok = tc_wait(cm, phase, A.status);
+                phase ^= 1u;
+                if (!ok) break;
+#pragma unroll
+                for (int c = 0; c < KP / 8; c++) {
+                    uint32_t ra[8], rb[8], r3[8], r4[8];
+                    tc::tmem_ld8(tbase + 8 * c, ra);
+                    tc::tmem_ld8(tbase + 16 + 8 * c, rb);
+                    tc::tmem_ld8(tbase + 32 + 8 * c, r3);
+                    tc::tmem_ld8(tbase + 48 + 8 * c, r4);
+                    tc::tmem_wait_ld32(ra, rb, r3, r4);
+#pragma unroll
+                    for (int i = 0; i < 8; i++) {
+                        const int a = 8 * c + i;
+                        ff s = {0.0f, 0.0f};
+                        if (a < L && x0 <= x1) {
+                            ff d2 = two_sum(__uint_as_float(ra[i]), __uint_as_float(rb[i]));
+                            ff t = two_sum(d2.hi, __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f));
+                            t.lo = __fadd_rn(t.lo, __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f, d2.lo));
+                            t = fast_two_sum(t.hi, t.lo);
+                            int E = vm + sm.gexp[a] - 2 * SLB + a * cm.p.sx;
+                            if (E >= -126 && vm > -1000 && sm.gexp[a] > -1000) s = ff_ldexp(t, E);
+                        }
+                        sm.S[m][a] = s;
+                    }
+                }
+                tc::fence_before_sync();
                 __syncthreads();
                 // stage 2 transposed: T[z][(b,a)] = sum_y S[(z,y)][a] Y[b][y]
                 for (int t = tid; t < TZ * npair; t += NTHR) {
@@ -523,8 +694,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     while (q >= L - b) { q -= L - b; b++; }
                     const int a = q;
                     ff s = {0.0f, 0.0f};
-                    for (int yy = 0; yy < TY; yy++) s = ff_fma(sm.S[zz * TY + yy][a], sm.Y[b][yy], s);
-                    sm.Cxy[zz][pair_index(L, b, a)] = s;
+                    for (int yy = 0; yy < TY; yy++) s = ff_fma(sm.S[zz * TY + yy][a], cm.Y[b][yy], s);
+                    cm.Cxy[zz][pair_index(L, b, a)] = s;
                 }
                 __syncthreads();
                 // stage 1 transposed: W[g][b][a] += sum_z T[z][(b,a)] Z[g][z]
@@ -547,13 +718,15 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     }
                     ff s = {0.0f, 0.0f};
                     const int pi = pair_index(L, b, a);
-                    for (int zz = 0; zz < TZ; zz++) s = ff_fma(sm.Cxy[zz][pi], sm.Z[g][zz], s);
+                    for (int zz = 0; zz < TZ; zz++) s = ff_fma(cm.Cxy[zz][pi], cm.Z[g][zz], s);
                     if (s.hi != 0.0f) atomicAdd(A.mom + moff + t, (double)s.hi + (double)s.lo);
                 }
                 __syncthreads();
             }
         }
+        if (cm.abort) break;
     }
+    tc_teardown(cm, kCols, phase);
 }
 
 __global__ void k_coef_to_ff(const double *__restrict__ c, float2 *__restrict__ out, int64_t n) {
@@ -659,15 +832,23 @@ int mixed_build(TaskSet &ts, std::string &err) {
     }
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P.device);
-    for (const void *fn : {(const void *)k_collocate_tiled, (const void *)k_integrate_tiled}) {
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem));
-        if (e != cudaSuccess) {
-            err = std::string("mixed_build: ") + cudaGetErrorString(e);
-            return GPW_ERR_CUDA;
-        }
+    e = cudaFuncSetAttribute((const void *)k_collocate_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)sizeof(SmemColl));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute((const void *)k_integrate_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(SmemInt));
+    if (e != cudaSuccess) {
+        err = std::string("mixed_build: ") + cudaGetErrorString(e);
+        return GPW_ERR_CUDA;
     }
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collocate_tiled, NTHR, sizeof(TileSmem));
-    M->grid_ctas = std::max(1, std::min(ntiles, sms * std::max(per_sm, 1)));
+    int per_sm_i = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collocate_tiled, NTHR, sizeof(SmemColl));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_i, k_integrate_tiled, NTHR, sizeof(SmemInt));
+    // TMEM: collocate CTAs hold 128 columns, integrate CTAs 64 (512 per SM)
+    per_sm = std::min(std::max(per_sm, 1), 4);
+    per_sm_i = std::min(std::max(per_sm_i, 1), 8);
+    M->grid_ctas_i = std::max(1, std::min(ntiles, sms * per_sm_i));
+    M->grid_ctas = std::max(1, std::min(ntiles, sms * per_sm));
     return GPW_SUCCESS;
 }
 
@@ -715,7 +896,7 @@ cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
         k_coef_to_ff<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(ts.d_coef, M.d_coef_ff, n);
         if ((e = cudaMemsetAsync(M.d_queue, 0, sizeof(int), s)) != cudaSuccess) return e;
         ProfScope prof(ts, s);
-        k_collocate_tiled<<<M.grid_ctas, NTHR, sizeof(TileSmem), s>>>(make_args(ts, g, 0));
+        k_collocate_tiled<<<M.grid_ctas, NTHR, sizeof(SmemColl), s>>>(make_args(ts, g, 0));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return general_fp64(ts, g, false, s);
@@ -728,7 +909,7 @@ cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
         if ((e = cudaMemsetAsync(ts.d_mom, 0, sizeof(double) * ts.coef_len, s)) != cudaSuccess) return e;
         if ((e = cudaMemsetAsync(M.d_queue + 1, 0, sizeof(int), s)) != cudaSuccess) return e;
         ProfScope prof(ts, s);
-        k_integrate_tiled<<<M.grid_ctas, NTHR, sizeof(TileSmem), s>>>(make_args(ts, g, 1));
+        k_integrate_tiled<<<M.grid_ctas_i, NTHR, sizeof(SmemInt), s>>>(make_args(ts, g, 1));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return general_fp64(ts, g, true, s);
