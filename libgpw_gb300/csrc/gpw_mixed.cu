@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -39,7 +40,7 @@ namespace gpw {
 constexpr int TX = 32, TY = 8, TZ = 16;
 constexpr int MROWS = TY * TZ;  // 128 rows per tile, one per thread
 constexpr int NTHR = MROWS;
-constexpr int NSL = 3;          // slices per operand
+constexpr int NSL = 4;          // slices per operand
 constexpr int SLB = 10;         // bits per slice
 constexpr int KP = 16;          // padded contraction length (alpha)
 constexpr int NPAIR_MAX = (kNPow * (kNPow + 1)) / 2;  // (b, a) with b + a <= lp
@@ -50,19 +51,6 @@ constexpr int kMaxImages = 4;  // periodic images of one cube axis over one tile
 struct TileDesc {
     int level;
     int t[3];  // tile indices
-};
-
-struct MixedState {
-    int ntiles = 0;
-    int64_t nitems = 0;
-    TileDesc *d_tiles = nullptr;
-    int64_t *d_start = nullptr;  // ntiles + 1
-    int *d_items = nullptr;      // sorted-task indices per tile
-    float2 *d_coef_ff = nullptr;
-    int *d_queue = nullptr;      // [0]: collocate, [1]: integrate
-    int northo = 0;              // ortho tasks come first in sorted order
-    int grid_ctas = 0;    // collocate
-    int grid_ctas_i = 0;  // integrate
 };
 
 // ---------------------------------------------------------------------------
@@ -79,8 +67,22 @@ struct TPair {
     int64_t coef_off, table_off;
     int o[3];           // cube offset of the tile origin (current image)
     int gx0, gx1;       // tile-local x range inside the cube box
-    int sx;             // x-variable rescale exponent of the current image
 };
+
+struct MixedState {
+    int ntiles = 0;
+    int64_t nitems = 0;
+    TileDesc *d_tiles = nullptr;
+    TPair *d_pairs = nullptr;    // per sorted task
+    int64_t *d_start = nullptr;  // ntiles + 1
+    int *d_items = nullptr;      // sorted-task indices per tile
+    float2 *d_coef_ff = nullptr;
+    int *d_queue = nullptr;      // [0]: collocate, [1]: integrate
+    int northo = 0;              // ortho tasks come first in sorted order
+    int grid_ctas = 0;    // collocate
+    int grid_ctas_i = 0;  // integrate
+};
+
 
 // ---------------------------------------------------------------------------
 // Sphere rule with an FP32 fast path.  The FP32 estimate decides unless it lies
@@ -150,19 +152,20 @@ __device__ __forceinline__ int slice_exponent(const ff *v, int n) {
 
 __device__ __forceinline__ void slice_value(ff v, int e, float *s) {
     if (e == -1000) {
-        s[0] = s[1] = s[2] = 0.0f;
+#pragma unroll
+        for (int i = 0; i < NSL; i++) s[i] = 0.0f;
         return;
     }
-    // v * 2^(SLB - e): |.| < 2^SLB
+    // v * 2^(SLB - e): |.| < 2^SLB; each later slice takes the next SLB bits
     const float hi = ldexpf(v.hi, SLB - e), lo = ldexpf(v.lo, SLB - e);
-    const float s1 = rintf(hi);
-    float r = __fadd_rn(__fsub_rn(hi, s1), lo);  // |r| <= 1/2 (+ tiny)
-    r = __fmul_rn(r, 1024.0f);
-    const float s2 = rintf(r);
-    r = __fmul_rn(__fsub_rn(r, s2), 1024.0f);
-    s[0] = s1;
-    s[1] = s2;
-    s[2] = rintf(r);
+    s[0] = rintf(hi);
+    float r = __fadd_rn(__fsub_rn(hi, s[0]), lo);  // |r| <= 1/2 (+ tiny)
+#pragma unroll
+    for (int i = 1; i < NSL; i++) {
+        r = __fmul_rn(r, 1024.0f);
+        s[i] = rintf(r);
+        r = __fsub_rn(r, s[i]);
+    }
 }
 
 // UMMA canonical K-major layout, no swizzle: core matrices of 8 rows x 16 bytes
@@ -173,17 +176,18 @@ __device__ __forceinline__ int umma_off(int r, int k) {
     return (r >> 3) * 256 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
-// Combine the diagonals of one product into float-float and scale by 2^E.
-__device__ __forceinline__ ff combine(float d2, float d3, float d4, int E) {
+// Combine the diagonals D_2..D_5 of one product (weights 1, 2^-10, 2^-20, 2^-30)
+// into float-float and scale by 2^E.
+__device__ __forceinline__ ff combine(float d2, float d3, float d4, float d5, int E) {
     ff s = two_sum(d2, __fmul_rn(d3, 0.0009765625f));
-    s.lo = __fmaf_rn(d4, 9.5367431640625e-07f, s.lo);
+    s.lo = __fmaf_rn(d4, 9.5367431640625e-07f, __fmaf_rn(d5, 9.313225746154785e-10f, s.lo));
     if (E < -126) return {0.0f, 0.0f};  // below 2^-102 of unit scale: dropped
     const float sc = __int_as_float((127 + E) << 23);
     return {__fmul_rn(s.hi, sc), __fmul_rn(s.lo, sc)};
 }
 
-// ---------------------------------------------------------------------------
 struct MixedArgs {
+    const TPair *pairs;
     const PairGeom *geoms;
     const LevelDev *levels;
     const TileDesc *tiles;
@@ -233,32 +237,13 @@ struct alignas(128) SmemInt {
 // pair index of (b, a), b + a <= lp, rows of constant b
 __device__ __forceinline__ int pair_index(int L, int b, int a) { return b * L - (b * (b - 1)) / 2 + a; }
 
-__device__ void load_pair(TileCommon &sm, const MixedArgs &A, const LevelDev &lv, int task) {
-    if (threadIdx.x == 0) {
-        const PairGeom &g = A.geoms[task];
-        TPair &p = sm.p;
-        p.r2 = rmul(g.radius, g.radius);
-        p.hx = lv.dh[0][0];
-        p.hy = lv.dh[1][1];
-        p.hz = lv.dh[2][2];
-        p.r2f = (float)p.r2;
-        p.hxf = (float)p.hx;
-        p.hyf = (float)p.hy;
-        p.hzf = (float)p.hz;
-        p.zetp = ff_from_double(g.zetp);
-        for (int d = 0; d < 3; d++) {
-            p.off[d] = ff_from_double(g.off[d]);
-            p.h[d] = ff_from_double(lv.dh[d][d]);
-            p.lb[d] = g.lb[d];
-            p.hi[d] = g.hi[d];
-            p.cc[d] = g.cc[d];
-        }
-        p.kgmin = g.kgmin;
-        p.lp = g.lp;
-        p.L = g.lp + 1;
-        p.coef_off = g.coef_off;
-        p.table_off = g.table_off;
-    }
+// The pair record is prepared on the host (float-float splits included) and
+// copied word by word; then the packed coefficients.
+__device__ void load_pair(TileCommon &sm, const MixedArgs &A, int task) {
+    static_assert(sizeof(TPair) % 4 == 0, "TPair must be word-sized");
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(A.pairs + task);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.p);
+    for (int t = threadIdx.x; t < (int)(sizeof(TPair) / 4); t += blockDim.x) dst[t] = src[t];
     __syncthreads();
     const int nc = ncoef(sm.p.lp);
     for (int t = threadIdx.x; t < nc; t += blockDim.x) sm.coef[t] = A.coef[sm.p.coef_off + t];
@@ -292,28 +277,19 @@ __device__ void axis_images(const LevelDev &lv, int d, int tt, int T, const TPai
     }
 }
 
-// Per image: tile origin in cube offsets, the x range inside the cube box, and
-// the power-of-two rescale of the x variable t -> t / 2^sx (|t / 2^sx| < 1 on
-// the tile), which balances the columns t^k exp(-zetp t^2) of stage 3.  The
-// factor 2^(k sx) goes to the row coefficients, so the product is unchanged.
+// Per image: tile origin in cube offsets and the x range inside the cube box.
 __device__ __forceinline__ void set_image(TPair &p, int ox, int oy, int oz, int ext_x) {
     p.o[0] = ox;
     p.o[1] = oy;
     p.o[2] = oz;
     p.gx0 = max(0, p.lb[0] - ox);
     p.gx1 = min(ext_x - 1, p.hi[0] - ox);
-    const float hx = p.h[0].hi, of = p.off[0].hi;
-    const float t0 = fabsf((float)(ox + p.gx0) * hx - of), t1 = fabsf((float)(ox + p.gx1) * hx - of);
-    int e = 0;
-    const float m = fmaxf(t0, t1);
-    if (m >= 1.0f) frexpf(m, &e);
-    p.sx = min(e, 30);
 }
 
-// tab[k][i] = (t/2^sx)^k exp(-zetp t^2), t = g h - off, g = o + i; zero outside the
-// cube box and outside the valid tile extent.
+// tab[k][i] = t^k exp(-zetp t^2), t = g h - off, g = o + i; zero outside the cube
+// box and outside the valid tile extent.
 __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool inside, ff *col, int stride,
-                                            int L, int sx) {
+                                            int L) {
     if (!inside) {
         for (int k = 0; k < KP; k++) col[k * stride] = ff{0.0f, 0.0f};
         return;
@@ -321,10 +297,9 @@ __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool i
     const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
     const ff a = ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo});
     ff e = ff_exp(a);
-    const ff ts = {ldexpf(t.hi, -sx), ldexpf(t.lo, -sx)};
     for (int k = 0; k < KP; k++) {
         col[k * stride] = k < L ? e : ff{0.0f, 0.0f};
-        if (k + 1 < L) e = ff_mul(e, ts);
+        if (k + 1 < L) e = ff_mul(e, t);
     }
 }
 
@@ -334,15 +309,15 @@ __device__ void build_tables(TileCommon &sm, const LevelDev &lv, const TileDesc 
     if (tid < TX) {
         const int g = p.o[0] + tid;
         const bool in = tid >= p.gx0 && tid <= p.gx1;
-        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L, p.sx);
+        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L);
     } else if (tid < TX + TY) {
         const int i = tid - TX, g = p.o[1] + i;
         const bool in = i < min(TY, lv.ngrid[1] - td.t[1] * TY) && g >= p.lb[1] && g <= p.hi[1];
-        table_entry(p, 1, g, in, &sm.Y[0][i], TY, p.L, 0);
+        table_entry(p, 1, g, in, &sm.Y[0][i], TY, p.L);
     } else if (tid < TX + TY + TZ) {
         const int i = tid - TX - TY, g = p.o[2] + i;
         const bool in = i < min(TZ, lv.ngrid[2] - td.t[2] * TZ) && g >= p.lb[2] && g <= p.hi[2];
-        table_entry(p, 2, g, in, &sm.Z[0][i], TZ, p.L, 0);
+        table_entry(p, 2, g, in, &sm.Z[0][i], TZ, p.L);
     }
 }
 
@@ -391,7 +366,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
     TileCommon &cm = sm.c;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m = tid, z = m / TY, y = m % TY;
-    constexpr uint32_t kCols = 128;  // D2, D3, D4: 32 columns each
+    constexpr uint32_t kCols = 128;  // diagonals D2..D5: 32 columns each
     tc_setup(cm, kCols);
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t idesc = tc::idesc_f16_f32(MROWS, TX);
@@ -409,7 +384,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
         for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
-            load_pair(cm, A, lv, A.items[it]);
+            load_pair(cm, A, A.items[it]);
             if (tid < 3) {
                 const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
                 axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
@@ -449,12 +424,11 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                     sm.fx[tid] = e;
 #pragma unroll
                     for (int k = 0; k < KP; k++) {
-                        float sl[3];
+                        float sl[NSL];
                         slice_value(col[k], e, sl);
                         const int o = umma_off(tid, k) >> 1;
-                        sm.B[0][o] = __float2half_rn(sl[0]);
-                        sm.B[1][o] = __float2half_rn(sl[1]);
-                        sm.B[2][o] = __float2half_rn(sl[2]);
+#pragma unroll
+                        for (int q = 0; q < NSL; q++) sm.B[q][o] = __float2half_rn(sl[q]);
                     }
                 }
                 __syncthreads();
@@ -470,18 +444,17 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                         if (a >= L) break;
                         ff s = {0.0f, 0.0f};
                         for (int b = 0; b <= lp - a; b++) s = ff_fma(cm.Cxy[z][pair_index(L, b, a)], cm.Y[b][y], s);
-                        cx[a] = ff_ldexp(s, a * cm.p.sx);
+                        cx[a] = s;
                     }
                 }
                 const int em = slice_exponent(cx, KP);
 #pragma unroll
                 for (int k = 0; k < KP; k++) {
-                    float sl[3];
+                    float sl[NSL];
                     slice_value(cx[k], em, sl);
                     const int o = umma_off(m, k) >> 1;
-                    sm.A[0][o] = __float2half_rn(sl[0]);
-                    sm.A[1][o] = __float2half_rn(sl[1]);
-                    sm.A[2][o] = __float2half_rn(sl[2]);
+#pragma unroll
+                    for (int q = 0; q < NSL; q++) sm.A[q][o] = __float2half_rn(sl[q]);
                 }
                 // stage 3 on the tensor cores: D_s = sum_{i+j=s} A_i B_j^T
                 tc::fence_async_smem();
@@ -489,17 +462,17 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                 __syncthreads();
                 if (tid == 0) {
                     tc::fence_after_sync();
-                    const uint64_t a0 = tc::desc_kmajor(sm.A[0], 128, 256), a1 = tc::desc_kmajor(sm.A[1], 128, 256),
-                                   a2 = tc::desc_kmajor(sm.A[2], 128, 256);
-                    const uint64_t b0 = tc::desc_kmajor(sm.B[0], 128, 256), b1 = tc::desc_kmajor(sm.B[1], 128, 256),
-                                   b2 = tc::desc_kmajor(sm.B[2], 128, 256);
-                    const uint32_t d = cm.tmem;
-                    tc::mma_f16(d, a0, b0, idesc, 0);
-                    tc::mma_f16(d + 32, a0, b1, idesc, 0);
-                    tc::mma_f16(d + 32, a1, b0, idesc, 1);
-                    tc::mma_f16(d + 64, a0, b2, idesc, 0);
-                    tc::mma_f16(d + 64, a1, b1, idesc, 1);
-                    tc::mma_f16(d + 64, a2, b0, idesc, 1);
+                    uint64_t ad[NSL], bd[NSL];
+#pragma unroll
+                    for (int q = 0; q < NSL; q++) {
+                        ad[q] = tc::desc_kmajor(sm.A[q], 128, 256);
+                        bd[q] = tc::desc_kmajor(sm.B[q], 128, 256);
+                    }
+                    // diagonal s = i + j into TMEM columns [32 s, 32 s + 32)
+#pragma unroll
+                    for (int sd = 0; sd < NSL; sd++)
+#pragma unroll
+                        for (int i = 0; i <= sd; i++) tc::mma_f16(cm.tmem + 32 * sd, ad[i], bd[sd - i], idesc, i > 0);
                     tc::mma_commit(&cm.mbar);
                 }
                 const bool ok = tc_wait(cm, phase, A.status);
@@ -507,20 +480,21 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                 if (!ok) break;
 #pragma unroll
                 for (int c = 0; c < TX / 8; c++) {
-                    uint32_t r2[8], r3[8], r4[8];
+                    uint32_t r2[8], r3[8], r4[8], r5[8];
                     tc::tmem_ld8(tbase + 8 * c, r2);
                     tc::tmem_ld8(tbase + 32 + 8 * c, r3);
                     tc::tmem_ld8(tbase + 64 + 8 * c, r4);
-                    tc::tmem_wait_ld24(r2, r3, r4);
+                    tc::tmem_ld8(tbase + 96 + 8 * c, r5);
+                    tc::tmem_wait_ld32(r2, r3, r4, r5);
 #pragma unroll
                     for (int i = 0; i < 8; i++) {
                         const int x = 8 * c + i;
                         if (x < x0 || x > x1) continue;
                         const ff v = combine(__uint_as_float(r2[i]), __uint_as_float(r3[i]), __uint_as_float(r4[i]),
-                                             em + sm.fx[x] - 2 * SLB);
-                        const ff s = two_sum(acc_hi[x], v.hi);
-                        acc_hi[x] = s.hi;
-                        acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(s.lo, v.lo));
+                                             __uint_as_float(r5[i]), em + sm.fx[x] - 2 * SLB);
+                        const ff sacc = two_sum(acc_hi[x], v.hi);
+                        acc_hi[x] = sacc.hi;
+                        acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(sacc.lo, v.lo));
                     }
                 }
                 tc::fence_before_sync();
@@ -549,7 +523,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
     TileCommon &cm = sm.c;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m = tid, z = m / TY, y = m % TY;
-    constexpr uint32_t kCols = 64;  // D2 (two K halves), D3, D4: 16 columns each
+    constexpr uint32_t kCols = 128;  // D2 (two K halves), D3, D4, D5: 16 columns each
     tc_setup(cm, kCols);
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t idesc = tc::idesc_f16_f32(MROWS, KP);
@@ -576,15 +550,14 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
             vm = slice_exponent(v, TX);
 #pragma unroll
             for (int x = 0; x < TX; x++) {
-                float sl[3];
+                float sl[NSL];
                 slice_value(v[x], vm, sl);
-                sm.Vs[0][m][x] = __float2half_rn(sl[0]);
-                sm.Vs[1][m][x] = __float2half_rn(sl[1]);
-                sm.Vs[2][m][x] = __float2half_rn(sl[2]);
+#pragma unroll
+                for (int q = 0; q < NSL; q++) sm.Vs[q][m][x] = __float2half_rn(sl[q]);
             }
         }
         for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
-            load_pair(cm, A, lv, A.items[it]);
+            load_pair(cm, A, A.items[it]);
             if (tid < 3) {
                 const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
                 axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
@@ -610,9 +583,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     const bool in = x >= x0 && x <= x1;
                     const int o = umma_off(m, x & 15) >> 1, h = x >> 4;
                     const __half zero = __float2half_rn(0.0f);
-                    sm.A[h][0][o] = in ? sm.Vs[0][m][x] : zero;
-                    sm.A[h][1][o] = in ? sm.Vs[1][m][x] : zero;
-                    sm.A[h][2][o] = in ? sm.Vs[2][m][x] : zero;
+#pragma unroll
+                    for (int q = 0; q < NSL; q++) sm.A[h][q][o] = in ? sm.Vs[q][m][x] : zero;
                 }
                 __syncthreads();
                 // B operand: X' slices per alpha over x (row exponent gexp[alpha])
@@ -625,12 +597,11 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     sm.gexp[a] = e;
 #pragma unroll
                     for (int x = 0; x < TX; x++) {
-                        float sl[3];
+                        float sl[NSL];
                         slice_value(row[x], e, sl);
                         const int o = umma_off(a, x & 15) >> 1, h = x >> 4;
-                        sm.B[h][0][o] = __float2half_rn(sl[0]);
-                        sm.B[h][1][o] = __float2half_rn(sl[1]);
-                        sm.B[h][2][o] = __float2half_rn(sl[2]);
+#pragma unroll
+                        for (int q = 0; q < NSL; q++) sm.B[h][q][o] = __float2half_rn(sl[q]);
                     }
                 }
                 tc::fence_async_smem();
@@ -638,25 +609,26 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                 __syncthreads();
                 if (tid == 0) {
                     tc::fence_after_sync();
-                    uint64_t a_[2][3], b_[2][3];
+                    uint64_t a_[2][NSL], b_[2][NSL];
                     for (int h = 0; h < 2; h++)
-                        for (int s2 = 0; s2 < 3; s2++) {
-                            a_[h][s2] = tc::desc_kmajor(sm.A[h][s2], 128, 256);
-                            b_[h][s2] = tc::desc_kmajor(sm.B[h][s2], 128, 256);
+                        for (int q = 0; q < NSL; q++) {
+                            a_[h][q] = tc::desc_kmajor(sm.A[h][q], 128, 256);
+                            b_[h][q] = tc::desc_kmajor(sm.B[h][q], 128, 256);
                         }
-                    const uint32_t d = cm.tmem;
-                    tc::mma_f16(d + 0, a_[0][0], b_[0][0], idesc, 0);   // D2, x in [0,16)
-                    tc::mma_f16(d + 16, a_[1][0], b_[1][0], idesc, 0);  // D2, x in [16,32)
-                    tc::mma_f16(d + 32, a_[0][0], b_[0][1], idesc, 0);  // D3
-                    tc::mma_f16(d + 32, a_[1][0], b_[1][1], idesc, 1);
-                    tc::mma_f16(d + 32, a_[0][1], b_[0][0], idesc, 1);
-                    tc::mma_f16(d + 32, a_[1][1], b_[1][0], idesc, 1);
-                    tc::mma_f16(d + 48, a_[0][0], b_[0][2], idesc, 0);  // D4
-                    tc::mma_f16(d + 48, a_[1][0], b_[1][2], idesc, 1);
-                    tc::mma_f16(d + 48, a_[0][1], b_[0][1], idesc, 1);
-                    tc::mma_f16(d + 48, a_[1][1], b_[1][1], idesc, 1);
-                    tc::mma_f16(d + 48, a_[0][2], b_[0][0], idesc, 1);
-                    tc::mma_f16(d + 48, a_[1][2], b_[1][0], idesc, 1);
+                    // D2 per K half (exact: 16 products each); diagonals 3.. over both halves
+                    tc::mma_f16(cm.tmem + 0, a_[0][0], b_[0][0], idesc, 0);
+                    tc::mma_f16(cm.tmem + 16, a_[1][0], b_[1][0], idesc, 0);
+#pragma unroll
+                    for (int sd = 1; sd < NSL; sd++) {
+                        int first = 1;
+#pragma unroll
+                        for (int i = 0; i <= sd; i++)
+#pragma unroll
+                            for (int h = 0; h < 2; h++) {
+                                tc::mma_f16(cm.tmem + 16 + 16 * sd, a_[h][i], b_[h][sd - i], idesc, first ? 0u : 1u);
+                                first = 0;
+                            }
+                    }
                     tc::mma_commit(&cm.mbar);
                 }
                 const bool ok = tc_wait(cm, phase, A.status);
@@ -664,22 +636,25 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                 if (!ok) break;
 #pragma unroll
                 for (int c = 0; c < KP / 8; c++) {
-                    uint32_t ra[8], rb[8], r3[8], r4[8];
+                    uint32_t ra[8], rb[8], r3[8], r4[8], r5[8];
                     tc::tmem_ld8(tbase + 8 * c, ra);
                     tc::tmem_ld8(tbase + 16 + 8 * c, rb);
                     tc::tmem_ld8(tbase + 32 + 8 * c, r3);
                     tc::tmem_ld8(tbase + 48 + 8 * c, r4);
                     tc::tmem_wait_ld32(ra, rb, r3, r4);
+                    tc::tmem_ld8(tbase + 64 + 8 * c, r5);
+                    tc::tmem_wait_ld8(r5);
 #pragma unroll
                     for (int i = 0; i < 8; i++) {
                         const int a = 8 * c + i;
                         ff s = {0.0f, 0.0f};
                         if (a < L && x0 <= x1) {
-                            ff d2 = two_sum(__uint_as_float(ra[i]), __uint_as_float(rb[i]));
+                            const ff d2 = two_sum(__uint_as_float(ra[i]), __uint_as_float(rb[i]));
                             ff t = two_sum(d2.hi, __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f));
-                            t.lo = __fadd_rn(t.lo, __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f, d2.lo));
+                            t.lo = __fadd_rn(t.lo, __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
+                                                             __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f, d2.lo)));
                             t = fast_two_sum(t.hi, t.lo);
-                            int E = vm + sm.gexp[a] - 2 * SLB + a * cm.p.sx;
+                            const int E = vm + sm.gexp[a] - 2 * SLB;
                             if (E >= -126 && vm > -1000 && sm.gexp[a] > -1000) s = ff_ldexp(t, E);
                         }
                         sm.S[m][a] = s;
@@ -815,6 +790,41 @@ int mixed_build(TaskSet &ts, std::string &err) {
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 16));
     };
+    std::vector<TPair> pairs((size_t)std::max<int64_t>(northo, 1));
+    auto split = [](double d) {
+        const float h = (float)d;
+        return ff{h, (float)(d - (double)h)};
+    };
+    for (int64_t k = 0; k < northo; k++) {
+        const PairGeom &g = ts.h_geom[k];
+        const LevelDev &lv = P.lv[g.level];
+        TPair &p = pairs[k];
+        memset(&p, 0, sizeof p);
+        p.r2 = rmul(g.radius, g.radius);
+        p.hx = lv.dh[0][0];
+        p.hy = lv.dh[1][1];
+        p.hz = lv.dh[2][2];
+        p.r2f = (float)p.r2;
+        p.hxf = (float)p.hx;
+        p.hyf = (float)p.hy;
+        p.hzf = (float)p.hz;
+        p.zetp = split(g.zetp);
+        for (int d = 0; d < 3; d++) {
+            p.off[d] = split(g.off[d]);
+            p.h[d] = split(lv.dh[d][d]);
+            p.lb[d] = g.lb[d];
+            p.hi[d] = g.hi[d];
+            p.cc[d] = g.cc[d];
+        }
+        p.kgmin = g.kgmin;
+        p.lp = g.lp;
+        p.L = g.lp + 1;
+        p.coef_off = g.coef_off;
+        p.table_off = g.table_off;
+    }
+    alloc((void **)&M->d_pairs, sizeof(TPair) * pairs.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(M->d_pairs, pairs.data(), sizeof(TPair) * pairs.size(), cudaMemcpyHostToDevice);
     alloc((void **)&M->d_tiles, sizeof(TileDesc) * ntiles);
     alloc((void **)&M->d_start, sizeof(int64_t) * (ntiles + 1));
     alloc((void **)&M->d_items, sizeof(int) * items.size());
@@ -844,9 +854,9 @@ int mixed_build(TaskSet &ts, std::string &err) {
     int per_sm_i = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collocate_tiled, NTHR, sizeof(SmemColl));
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_i, k_integrate_tiled, NTHR, sizeof(SmemInt));
-    // TMEM: collocate CTAs hold 128 columns, integrate CTAs 64 (512 per SM)
+    // TMEM: every CTA holds 128 columns (512 per SM)
     per_sm = std::min(std::max(per_sm, 1), 4);
-    per_sm_i = std::min(std::max(per_sm_i, 1), 8);
+    per_sm_i = std::min(std::max(per_sm_i, 1), 4);
     M->grid_ctas_i = std::max(1, std::min(ntiles, sms * per_sm_i));
     M->grid_ctas = std::max(1, std::min(ntiles, sms * per_sm));
     return GPW_SUCCESS;
@@ -856,6 +866,7 @@ void mixed_free(TaskSet &ts) {
     MixedState *M = ts.mixed;
     if (!M) return;
     cudaFree(M->d_tiles);
+    cudaFree(M->d_pairs);
     cudaFree(M->d_start);
     cudaFree(M->d_items);
     cudaFree(M->d_coef_ff);
@@ -867,6 +878,7 @@ void mixed_free(TaskSet &ts) {
 static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which) {
     const MixedState &M = *ts.mixed;
     MixedArgs a;
+    a.pairs = M.d_pairs;
     a.geoms = ts.d_geom;
     a.levels = ts.plan->d_levels;
     a.tiles = M.d_tiles;
