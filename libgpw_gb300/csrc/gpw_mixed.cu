@@ -176,6 +176,30 @@ __device__ __forceinline__ int umma_off(int r, int k) {
     return (r >> 3) * 256 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2;
 }
 
+constexpr int kZeroExp = -1000;
+// 2^k as a float, -126 <= k <= 127
+__device__ __forceinline__ float pow2i(int k) { return __int_as_float((127 + k) << 23); }
+// e with m = f 2^e, f in [0.5, 1); values below 2^-100 count as zero
+__device__ __forceinline__ int exp_of(float m) {
+    return m >= 7.888609052210118e-31f ? ((__float_as_int(m) >> 23) & 0xff) - 126 : kZeroExp;
+}
+// the NSL fixed-point slices of v * scale, scale = 2^(SLB - e)
+__device__ __forceinline__ void slice_scaled(ff v, float scale, float *sl) {
+    const float hi = __fmul_rn(v.hi, scale), lo = __fmul_rn(v.lo, scale);
+    sl[0] = rintf(hi);
+    float r = __fadd_rn(__fsub_rn(hi, sl[0]), lo);
+#pragma unroll
+    for (int i = 1; i < NSL; i++) {
+        r = __fmul_rn(r, 1024.0f);
+        sl[i] = rintf(r);
+        r = __fsub_rn(r, sl[i]);
+    }
+}
+// two consecutive K entries (k even) of one operand row as packed halves
+__device__ __forceinline__ void store_pair(__half *base, int r, int k, float a, float b) {
+    *reinterpret_cast<__half2 *>(base + (umma_off(r, k) >> 1)) = __floats2half2_rn(a, b);
+}
+
 // Combine the diagonals D_2..D_5 of one product (weights 1, 2^-10, 2^-20, 2^-30)
 // into float-float and scale by 2^E.
 __device__ __forceinline__ ff combine(float d2, float d3, float d4, float d5, int E) {
@@ -220,8 +244,9 @@ struct TileCommon {
 
 struct alignas(128) SmemColl {
     __half A[NSL][MROWS * KP];  // Cx slices, M=128 x K=16
-    __half B[NSL][TX * KP];     // X' slices, N=32 x K=16
-    int fx[TX];
+    __half B[NSL][TX * KP];     // X slices, N=32 x K=16
+    ff cxs[KP][MROWS];          // stage-2 rows (column m belongs to thread m)
+    float cs[TX];               // 2^fx per column (0 for an empty column)
     TileCommon c;
 };
 
@@ -360,7 +385,7 @@ __device__ __forceinline__ bool tc_wait(TileCommon &c, uint32_t phase, int *stat
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
+__global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemColl &sm = *reinterpret_cast<SmemColl *>(smraw);
     TileCommon &cm = sm.c;
@@ -383,7 +408,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
         for (int x = 0; x < TX; x++) acc_hi[x] = acc_lo[x] = 0.0f;
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
-        for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
+        const int64_t it_end = A.start[tile + 1];
+        for (int64_t it = A.start[tile]; it < it_end && !cm.abort; it++) {
             load_pair(cm, A, A.items[it]);
             if (tid < 3) {
                 const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
@@ -405,7 +431,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                 const int npair = (L * (L + 1)) / 2;
                 for (int t = tid; t < TZ * npair; t += NTHR) {
                     const int zz = t / npair;
-                    int q = t % npair, b = 0;
+                    int q = t - zz * npair, b = 0;
                     while (q >= L - b) { q -= L - b; b++; }
                     const int a = q;
                     ff s = {0.0f, 0.0f};
@@ -415,46 +441,46 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                     }
                     cm.Cxy[zz][pair_index(L, b, a)] = s;
                 }
-                // B slices: column x over alpha
+                // B slices: column x over alpha, scaled by 2^(SLB - fx)
                 if (tid < TX) {
-                    ff col[KP];
+                    float mx = 0.0f;
+                    for (int k = 0; k < L; k++) mx = fmaxf(mx, fabsf(cm.X[k][tid].hi));
+                    const int e = exp_of(mx);
+                    sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
+                    const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
 #pragma unroll
-                    for (int k = 0; k < KP; k++) col[k] = cm.X[k][tid];
-                    const int e = slice_exponent(col, KP);
-                    sm.fx[tid] = e;
+                    for (int k = 0; k < KP; k += 2) {
+                        float s0[NSL], s1[NSL];
+                        slice_scaled(k < L ? cm.X[k][tid] : ff{0.0f, 0.0f}, sc, s0);
+                        slice_scaled(k + 1 < L ? cm.X[k + 1][tid] : ff{0.0f, 0.0f}, sc, s1);
 #pragma unroll
-                    for (int k = 0; k < KP; k++) {
-                        float sl[NSL];
-                        slice_value(col[k], e, sl);
-                        const int o = umma_off(tid, k) >> 1;
-#pragma unroll
-                        for (int q = 0; q < NSL; q++) sm.B[q][o] = __float2half_rn(sl[q]);
+                        for (int q = 0; q < NSL; q++) store_pair(sm.B[q], tid, k, s0[q], s1[q]);
                     }
                 }
                 __syncthreads();
-                // stage 2 + row culling + A slices (thread = row)
+                // stage 2 (this thread's row) + culling + A slices
                 int x0, x1;
                 row_range(cm.p, A.table, cm.p.o[2] + z, cm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
-                ff cx[KP];
-#pragma unroll
-                for (int a = 0; a < KP; a++) cx[a] = ff{0.0f, 0.0f};
+                float mx = 0.0f;
                 if (x0 <= x1) {
-#pragma unroll
-                    for (int a = 0; a < KP; a++) {
-                        if (a >= L) break;
+                    for (int a = 0; a < L; a++) {
                         ff s = {0.0f, 0.0f};
                         for (int b = 0; b <= lp - a; b++) s = ff_fma(cm.Cxy[z][pair_index(L, b, a)], cm.Y[b][y], s);
-                        cx[a] = s;
+                        sm.cxs[a][m] = s;
+                        mx = fmaxf(mx, fabsf(s.hi));
                     }
                 }
-                const int em = slice_exponent(cx, KP);
+                const int em = exp_of(mx);
+                {
+                    const float sc = em == kZeroExp ? 0.0f : pow2i(SLB - em);
 #pragma unroll
-                for (int k = 0; k < KP; k++) {
-                    float sl[NSL];
-                    slice_value(cx[k], em, sl);
-                    const int o = umma_off(m, k) >> 1;
+                    for (int k = 0; k < KP; k += 2) {
+                        float s0[NSL], s1[NSL];
+                        slice_scaled(k < L && em != kZeroExp ? sm.cxs[k][m] : ff{0.0f, 0.0f}, sc, s0);
+                        slice_scaled(k + 1 < L && em != kZeroExp ? sm.cxs[k + 1][m] : ff{0.0f, 0.0f}, sc, s1);
 #pragma unroll
-                    for (int q = 0; q < NSL; q++) sm.A[q][o] = __float2half_rn(sl[q]);
+                        for (int q = 0; q < NSL; q++) store_pair(sm.A[q], m, k, s0[q], s1[q]);
+                    }
                 }
                 // stage 3 on the tensor cores: D_s = sum_{i+j=s} A_i B_j^T
                 tc::fence_async_smem();
@@ -478,23 +504,37 @@ __global__ void __launch_bounds__(NTHR, 2) k_collocate_tiled(MixedArgs A) {
                 const bool ok = tc_wait(cm, phase, A.status);
                 phase ^= 1u;
                 if (!ok) break;
+                // tcgen05.ld is warp-collective: chunk decisions are made per warp
+                if (__any_sync(0xffffffffu, x0 <= x1)) {
+                    const float rs = pow2i(max(em - 2 * SLB, -126));
 #pragma unroll
-                for (int c = 0; c < TX / 8; c++) {
-                    uint32_t r2[8], r3[8], r4[8], r5[8];
-                    tc::tmem_ld8(tbase + 8 * c, r2);
-                    tc::tmem_ld8(tbase + 32 + 8 * c, r3);
-                    tc::tmem_ld8(tbase + 64 + 8 * c, r4);
-                    tc::tmem_ld8(tbase + 96 + 8 * c, r5);
-                    tc::tmem_wait_ld32(r2, r3, r4, r5);
+                    for (int c = 0; c < TX / 8; c++) {
+                        if (!__any_sync(0xffffffffu, x0 <= x1 && 8 * c <= x1 && 8 * c + 7 >= x0)) continue;
+                        uint32_t r2[8], r3[8], r4[8], r5[8];
+                        tc::tmem_ld8(tbase + 8 * c, r2);
+                        tc::tmem_ld8(tbase + 32 + 8 * c, r3);
+                        tc::tmem_ld8(tbase + 64 + 8 * c, r4);
+                        tc::tmem_ld8(tbase + 96 + 8 * c, r5);
+                        tc::tmem_wait_ld32(r2, r3, r4, r5);
 #pragma unroll
-                    for (int i = 0; i < 8; i++) {
-                        const int x = 8 * c + i;
-                        if (x < x0 || x > x1) continue;
-                        const ff v = combine(__uint_as_float(r2[i]), __uint_as_float(r3[i]), __uint_as_float(r4[i]),
-                                             __uint_as_float(r5[i]), em + sm.fx[x] - 2 * SLB);
-                        const ff sacc = two_sum(acc_hi[x], v.hi);
-                        acc_hi[x] = sacc.hi;
-                        acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(sacc.lo, v.lo));
+                        for (int i = 0; i < 8; i++) {
+                            const int x = 8 * c + i;
+                            if (x < x0 || x > x1) continue;
+                            const float d2 = __uint_as_float(r2[i]);
+                            const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
+                                               __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
+                                                         __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
+                            float hi = __fadd_rn(d2, corr);
+                            float lo = __fsub_rn(corr, __fsub_rn(hi, d2));
+                            const float scl = __fmul_rn(rs, sm.cs[x]);
+                            hi = __fmul_rn(hi, scl);
+                            lo = __fmul_rn(lo, scl);
+                            const float s = __fadd_rn(acc_hi[x], hi);
+                            const float bb = __fsub_rn(s, acc_hi[x]);
+                            const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(s, bb)), __fsub_rn(hi, bb));
+                            acc_hi[x] = s;
+                            acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
+                        }
                     }
                 }
                 tc::fence_before_sync();
