@@ -81,6 +81,7 @@ struct MixedState {
     int northo = 0;              // ortho tasks come first in sorted order
     int grid_ctas = 0;    // collocate
     int grid_ctas_i = 0;  // integrate
+    int per_sm = 0, per_sm_i = 0;
 };
 
 
@@ -138,34 +139,6 @@ __device__ __forceinline__ void row_range(const TPair &p, const int *table, int 
     // cube offsets [imin, 1 - imin] -> tile-local
     x0 = max(imin - p.o[0], p.gx0);
     x1 = min(1 - imin - p.o[0], p.gx1);
-}
-
-// ---------------------------------------------------------------------------
-// fixed-point slicing of one vector (n entries, float-float) into NSL slices
-__device__ __forceinline__ int slice_exponent(const ff *v, int n) {
-    float m = 0.0f;
-    for (int a = 0; a < n; a++) m = fmaxf(m, fabsf(v[a].hi));
-    int e = 0;
-    if (m > 0.0f) frexpf(m, &e);  // m = f * 2^e, f in [0.5, 1)
-    return m > 0.0f ? e : -1000;
-}
-
-__device__ __forceinline__ void slice_value(ff v, int e, float *s) {
-    if (e == -1000) {
-#pragma unroll
-        for (int i = 0; i < NSL; i++) s[i] = 0.0f;
-        return;
-    }
-    // v * 2^(SLB - e): |.| < 2^SLB; each later slice takes the next SLB bits
-    const float hi = ldexpf(v.hi, SLB - e), lo = ldexpf(v.lo, SLB - e);
-    s[0] = rintf(hi);
-    float r = __fadd_rn(__fsub_rn(hi, s[0]), lo);  // |r| <= 1/2 (+ tiny)
-#pragma unroll
-    for (int i = 1; i < NSL; i++) {
-        r = __fmul_rn(r, 1024.0f);
-        s[i] = rintf(r);
-        r = __fsub_rn(r, s[i]);
-    }
 }
 
 // UMMA canonical K-major layout, no swizzle: core matrices of 8 rows x 16 bytes
@@ -346,7 +319,6 @@ __device__ void build_tables(TileCommon &sm, const LevelDev &lv, const TileDesc 
     }
 }
 
-__device__ __forceinline__ ff ff_ldexp(ff v, int e) { return {ldexpf(v.hi, e), ldexpf(v.lo, e)}; }
 
 // TMEM set-up shared by both kernels: warp 0 allocates, thread 0 inits the mbarrier
 __device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
@@ -587,13 +559,19 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
             ff v[TX];
 #pragma unroll
             for (int x = 0; x < TX; x++) v[x] = (ok && x < ext_x) ? ff_from_double(grid[row + x]) : ff{0.0f, 0.0f};
-            vm = slice_exponent(v, TX);
+            float mx = 0.0f;
 #pragma unroll
-            for (int x = 0; x < TX; x++) {
-                float sl[NSL];
-                slice_value(v[x], vm, sl);
+            for (int x = 0; x < TX; x++) mx = fmaxf(mx, fabsf(v[x].hi));
+            vm = exp_of(mx);
+            const float sc = vm == kZeroExp ? 0.0f : pow2i(SLB - vm);
 #pragma unroll
-                for (int q = 0; q < NSL; q++) sm.Vs[q][m][x] = __float2half_rn(sl[q]);
+            for (int x = 0; x < TX; x += 2) {
+                float s0[NSL], s1[NSL];
+                slice_scaled(v[x], sc, s0);
+                slice_scaled(v[x + 1], sc, s1);
+#pragma unroll
+                for (int q = 0; q < NSL; q++)
+                    *reinterpret_cast<__half2 *>(&sm.Vs[q][m][x]) = __floats2half2_rn(s0[q], s1[q]);
             }
         }
         for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
@@ -619,29 +597,36 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                 int x0, x1;
                 row_range(cm.p, A.table, cm.p.o[2] + z, cm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
 #pragma unroll
-                for (int x = 0; x < TX; x++) {
-                    const bool in = x >= x0 && x <= x1;
+                for (int x = 0; x < TX; x += 2) {
+                    const bool in0 = x >= x0 && x <= x1, in1 = x + 1 >= x0 && x + 1 <= x1;
                     const int o = umma_off(m, x & 15) >> 1, h = x >> 4;
-                    const __half zero = __float2half_rn(0.0f);
 #pragma unroll
-                    for (int q = 0; q < NSL; q++) sm.A[h][q][o] = in ? sm.Vs[q][m][x] : zero;
+                    for (int q = 0; q < NSL; q++) {
+                        __half2 v2 = *reinterpret_cast<const __half2 *>(&sm.Vs[q][m][x]);
+                        if (!in0) v2.x = __float2half_rn(0.0f);
+                        if (!in1) v2.y = __float2half_rn(0.0f);
+                        *reinterpret_cast<__half2 *>(&sm.A[h][q][o]) = v2;
+                    }
                 }
                 __syncthreads();
-                // B operand: X' slices per alpha over x (row exponent gexp[alpha])
+                // B operand: X slices per alpha over x (row exponent gexp[alpha])
                 if (tid < KP) {
                     const int a = tid;
-                    ff row[TX];
+                    float mxb = 0.0f;
 #pragma unroll
-                    for (int x = 0; x < TX; x++) row[x] = cm.X[a][x];
-                    const int e = slice_exponent(row, TX);
+                    for (int x = 0; x < TX; x++) mxb = fmaxf(mxb, fabsf(cm.X[a][x].hi));
+                    const int e = exp_of(mxb);
                     sm.gexp[a] = e;
+                    const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
 #pragma unroll
-                    for (int x = 0; x < TX; x++) {
-                        float sl[NSL];
-                        slice_value(row[x], e, sl);
+                    for (int x = 0; x < TX; x += 2) {
+                        float s0[NSL], s1[NSL];
+                        slice_scaled(cm.X[a][x], sc, s0);
+                        slice_scaled(cm.X[a][x + 1], sc, s1);
                         const int o = umma_off(a, x & 15) >> 1, h = x >> 4;
 #pragma unroll
-                        for (int q = 0; q < NSL; q++) sm.B[h][q][o] = __float2half_rn(sl[q]);
+                        for (int q = 0; q < NSL; q++)
+                            *reinterpret_cast<__half2 *>(&sm.B[h][q][o]) = __floats2half2_rn(s0[q], s1[q]);
                     }
                 }
                 tc::fence_async_smem();
@@ -695,7 +680,10 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                                                              __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f, d2.lo)));
                             t = fast_two_sum(t.hi, t.lo);
                             const int E = vm + sm.gexp[a] - 2 * SLB;
-                            if (E >= -126 && vm > -1000 && sm.gexp[a] > -1000) s = ff_ldexp(t, E);
+                            if (E >= -126 && vm != kZeroExp && sm.gexp[a] != kZeroExp) {
+                                const float scl = pow2i(min(E, 127));
+                                s = {__fmul_rn(t.hi, scl), __fmul_rn(t.lo, scl)};
+                            }
                         }
                         sm.S[m][a] = s;
                     }
@@ -891,12 +879,22 @@ int mixed_build(TaskSet &ts, std::string &err) {
         err = std::string("mixed_build: ") + cudaGetErrorString(e);
         return GPW_ERR_CUDA;
     }
-    int per_sm_i = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collocate_tiled, NTHR, sizeof(SmemColl));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_i, k_integrate_tiled, NTHR, sizeof(SmemInt));
-    // TMEM: every CTA holds 128 columns (512 per SM)
-    per_sm = std::min(std::max(per_sm, 1), 4);
-    per_sm_i = std::min(std::max(per_sm_i, 1), 4);
+    // resident CTAs per SM from the kernels' own resources; TMEM (128 of 512
+    // columns per CTA) caps it at 4
+    auto resident = [&](const void *fn, size_t dyn) {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess) return 1;
+        int smem_sm = 0, regs_sm = 0;
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, P.device);
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, P.device);
+        const int by_regs = regs_sm / std::max(1, ((fa.numRegs * 32 + 255) / 256) * 256 * (NTHR / 32));
+        const int by_smem = (int)(smem_sm / (dyn + fa.sharedSizeBytes + 1024));
+        return std::max(1, std::min({by_regs, by_smem, 4}));
+    };
+    per_sm = resident((const void *)k_collocate_tiled, sizeof(SmemColl));
+    const int per_sm_i = resident((const void *)k_integrate_tiled, sizeof(SmemInt));
+    M->per_sm = per_sm;
+    M->per_sm_i = per_sm_i;
     M->grid_ctas_i = std::max(1, std::min(ntiles, sms * per_sm_i));
     M->grid_ctas = std::max(1, std::min(ntiles, sms * per_sm));
     return GPW_SUCCESS;
