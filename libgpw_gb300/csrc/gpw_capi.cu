@@ -395,16 +395,20 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
     T->pab_extent = extent;
     T->h_geom.resize((size_t)ntasks);
     int64_t coef = 0;
+    int64_t mom_ext = 0;
     for (int64_t k = 0; k < ntasks; k++) {
         PairGeom g = geo[order[k]];
         g.coef_off = coef;
         coef += ncoef(g.lp);
+        g.mom_ext_off = mom_ext;
+        mom_ext += ncoef(std::min(g.lp + 2, kMaxLp));
         T->max_lp = std::max(T->max_lp, g.lp);
         T->max_A = std::max(T->max_A, g.la_max);
         T->max_B = std::max(T->max_B, g.lb_max);
         T->h_geom[k] = g;
     }
     T->coef_len = coef;
+    T->mom_ext_len = mom_ext;
     // FP64 launch chunks: similar shared-memory needs launch together
     int64_t k = 0;
     int smem_limit = 0;
@@ -414,9 +418,12 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
         c.first = (int)k;
         c.kind = T->h_geom[k].ortho ? 0 : 1;
         c.smem_bytes = 0;
+        c.smem_ext = 0;
         int64_t m = k;
         while (m < ntasks && (T->h_geom[m].ortho ? 0 : 1) == c.kind) {
             const int need = c.kind == 0 ? smem_ortho_fp64(T->h_geom[m]) : smem_general_fp64(T->h_geom[m]);
+            const int need_ext = c.kind == 0 ? smem_ortho_fp64(T->h_geom[m], 2) : smem_general_fp64(T->h_geom[m], 2);
+            c.smem_ext = std::max(c.smem_ext, std::min(need_ext, smem_limit));
             if (need > smem_limit) {
                 delete T;
                 return fail(GPW_ERR_UNSUPPORTED, "gpw_taskset_create: a cube is too large for one CTA");
@@ -478,6 +485,7 @@ int gpw_taskset_destroy(gpw_taskset *ts) {
     cudaFree(ts->d_table);
     cudaFree(ts->d_coef);
     cudaFree(ts->d_mom);
+    cudaFree(ts->d_mom_ext);
     cudaFree(ts->d_status);
     delete ts;
     return GPW_SUCCESS;

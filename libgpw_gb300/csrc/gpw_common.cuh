@@ -154,6 +154,7 @@ struct PairGeom {
     int64_t coef_off;  // scratch offset of the packed coefficients
     int64_t table_off; // CP2K-format cube list (ortho), -1: sphere rule
     int64_t cost;      // estimated cube points
+    int64_t mom_ext_off; // scratch offset of the degree lp+2 moments (backward)
     double zeta, zetb;
 };
 

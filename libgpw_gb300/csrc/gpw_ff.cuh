@@ -56,8 +56,16 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
     return fast_two_sum(p, e);
 }
 
-// a*b + c
-__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) { return ff_add(ff_mul(a, b), c); }
+// a*b + c in one pass: exact product error by FMA, exact sum with c.hi, one renormalisation
+__device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const ff s = two_sum(p, c.hi);
+    const float t = __fadd_rn(s.lo, __fadd_rn(e, c.lo));
+    return fast_two_sum(s.hi, t);
+}
 
 // exp(a) for -87 < a.hi < 80.  Cody-Waite reduction r = a - k ln2 with ln2 split
 // as L1 (16 significant bits, so k*L1 is exact for |k| < 2^8) plus a float-float

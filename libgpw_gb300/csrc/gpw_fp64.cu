@@ -153,8 +153,8 @@ __global__ void k_backtransform(const PairGeom *__restrict__ geoms, const LevelD
 
 // ---------------------------------------------------------------------------
 // orthorhombic collocate, one CTA per pair
-int smem_ortho_fp64(const PairGeom &g) {
-    const int L = g.lp + 1;
+int smem_ortho_fp64(const PairGeom &g, int extra) {
+    const int L = g.lp + 1 + extra;
     const int nx = g.hi[0] - g.lb[0] + 1, ny = g.hi[1] - g.lb[1] + 1, nz = g.hi[2] - g.lb[2] + 1;
     return 8 * (L * L * L + L * (nx + ny + nz) + L * L + ny * L) + 8 * ny;
 }
@@ -163,12 +163,13 @@ template <bool kAdj>
 __global__ void __launch_bounds__(256)
 k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__restrict__ levels,
              const int *__restrict__ table, const double *__restrict__ coef, double *__restrict__ mom,
-             GridPtrs grids, int *status) {
+             GridPtrs grids, int *status, int extra) {
     extern __shared__ double sm[];
     const PairGeom g = geoms[first + blockIdx.x];
     const LevelDev &lv = levels[g.level];
     double *__restrict__ grid = grids.p[g.level];
-    const int lp = g.lp, L = lp + 1;
+    const int lp = g.lp + extra, L = lp + 1;
+    const int64_t mom_off = extra ? g.mom_ext_off : g.coef_off;
     const int nx = g.hi[0] - g.lb[0] + 1, ny = g.hi[1] - g.lb[1] + 1, nz = g.hi[2] - g.lb[2] + 1;
     double *C = sm;                // [lz][ly][lx] dense: coefficients, or moments (adjoint)
     double *Xt = C + L * L * L;    // [k][gi]
@@ -283,7 +284,7 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
     if (kAdj) {
         for (int t = tid; t < L * L * L; t += nthr) {
             const int lx = t % L, ly = (t / L) % L, lz = t / (L * L);
-            if (lx + ly + lz <= lp) mom[g.coef_off + pidx(lp, lz, ly, lx)] = C[t];
+            if (lx + ly + lz <= lp) mom[mom_off + pidx(lp, lz, ly, lx)] = C[t];
         }
     }
 }
@@ -311,8 +312,8 @@ GPW_HD bool general_row(const double dh[3][3], const double gp[3], double dj, do
     return true;
 }
 
-int smem_general_fp64(const PairGeom &g) {
-    const int L = g.lp + 1;
+int smem_general_fp64(const PairGeom &g, int extra) {
+    const int L = g.lp + 1 + extra;
     const int ny = g.hi[1] - g.cc[1] + 1;
     return 8 * (L * L * L + L * L + ny * L) + 12 * ny;
 }
@@ -321,12 +322,13 @@ template <bool kAdj>
 __global__ void __launch_bounds__(256)
 k_general_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__restrict__ levels,
                const double *__restrict__ coef, double *__restrict__ mom, GridPtrs grids,
-               int *status) {
+               int *status, int extra) {
     extern __shared__ double sm[];
     const PairGeom g = geoms[first + blockIdx.x];
     const LevelDev &lv = levels[g.level];
     double *__restrict__ grid = grids.p[g.level];
-    const int lp = g.lp, L = lp + 1;
+    const int lp = g.lp + extra, L = lp + 1;
+    const int64_t mom_off = extra ? g.mom_ext_off : g.coef_off;
     const int ny = g.hi[1] - g.cc[1] + 1;
     double *Q = sm;              // [k][j][i] dense
     double *Qjk = Q + L * L * L; // [j][i]
@@ -460,7 +462,7 @@ k_general_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__
     if (kAdj) {
         for (int t = tid; t < L * L * L; t += nthr) {
             const int i = t % L, j = (t / L) % L, k = t / (L * L);
-            if (i + j + k <= lp) mom[g.coef_off + pidx(lp, k, j, i)] = Q[t];
+            if (i + j + k <= lp) mom[mom_off + pidx(lp, k, j, i)] = Q[t];
         }
     }
 }
@@ -481,8 +483,11 @@ cudaError_t launch_prep(const TaskSet &ts, const double *d_pab, cudaStream_t s) 
     return cudaGetLastError();
 }
 
-cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, cudaStream_t s) {
-    for (const Chunk &c : ts.chunks) {
+static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, int extra,
+                                    double *mom, cudaStream_t s) {
+    for (const Chunk &c0 : ts.chunks) {
+        Chunk c = c0;
+        if (extra) c.smem_bytes = c0.smem_ext;
         if (c.count == 0 || (kind >= 0 && c.kind != kind)) continue;
         const void *fn;
         if (c.kind == 0)
@@ -495,24 +500,32 @@ cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int
         if (c.kind == 0) {
             if (adj)
                 k_ortho_fp64<true><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
-                                                                     ts.d_table, ts.d_coef, ts.d_mom, g,
-                                                                     ts.d_status);
+                                                                     ts.d_table, ts.d_coef, mom, g,
+                                                                     ts.d_status, extra);
             else
                 k_ortho_fp64<false><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
-                                                                      ts.d_table, ts.d_coef, ts.d_mom, g,
-                                                                      ts.d_status);
+                                                                      ts.d_table, ts.d_coef, mom, g,
+                                                                      ts.d_status, 0);
         } else {
             if (adj)
                 k_general_fp64<true><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
-                                                                       ts.d_coef, ts.d_mom, g, ts.d_status);
+                                                                       ts.d_coef, mom, g, ts.d_status, extra);
             else
                 k_general_fp64<false><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
-                                                                        ts.d_coef, ts.d_mom, g, ts.d_status);
+                                                                        ts.d_coef, mom, g, ts.d_status, 0);
         }
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, cudaStream_t s) {
+    return launch_fp64_impl(ts, g, adj, kind, 0, ts.d_mom, s);
+}
+
+cudaError_t launch_moments_fp64(const TaskSet &ts, const GridPtrs &g, int extra, double *out, cudaStream_t s) {
+    return launch_fp64_impl(ts, g, true, -1, extra, out, s);
 }
 
 cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {

@@ -18,7 +18,8 @@ struct GridPtrs {
 struct Chunk {
     int first, count;
     int smem_bytes;
-    int kind;  // 0 ortho, 1 general
+    int smem_ext;  // with two extra powers (backward moments)
+    int kind;      // 0 ortho, 1 general
 };
 
 struct Plan {
@@ -45,6 +46,8 @@ struct TaskSet {
     double *d_coef = nullptr;      // packed coefficients, per call
     double *d_mom = nullptr;       // packed moments (integrate), per call
     int64_t coef_len = 0;
+    int64_t mom_ext_len = 0;
+    double *d_mom_ext = nullptr;   // backward: moments up to degree lp + 2
     int *d_status = nullptr;
     std::vector<Chunk> chunks;     // FP64 launches
     MixedState *mixed = nullptr;
@@ -86,8 +89,10 @@ cudaError_t launch_integrate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStre
 cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, cudaStream_t s);
 cudaError_t launch_backtransform(const TaskSet &ts, const double *d_mom, double *d_hab,
                                  cudaStream_t s);
-int smem_ortho_fp64(const PairGeom &g);
-int smem_general_fp64(const PairGeom &g);
+int smem_ortho_fp64(const PairGeom &g, int extra = 0);
+int smem_general_fp64(const PairGeom &g, int extra = 0);
+// moments <V | t^k...> up to degree lp + extra into out (offsets coef_off, or mom_ext_off when extra > 0)
+cudaError_t launch_moments_fp64(const TaskSet &ts, const GridPtrs &g, int extra, double *out, cudaStream_t s);
 int smem_prep(int A, int B);
 
 // gpw_core.cu

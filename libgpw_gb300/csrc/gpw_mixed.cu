@@ -413,20 +413,25 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     }
                     cm.Cxy[zz][pair_index(L, b, a)] = s;
                 }
-                // B slices: column x over alpha, scaled by 2^(SLB - fx)
-                if (tid < TX) {
+                // B slices: column x over alpha, scaled by 2^(SLB - fx); four threads per column
+                {
+                    const int x = tid >> 2, k0 = (tid & 3) * 4;
                     float mx = 0.0f;
-                    for (int k = 0; k < L; k++) mx = fmaxf(mx, fabsf(cm.X[k][tid].hi));
+#pragma unroll
+                    for (int k = k0; k < k0 + 4; k++)
+                        if (k < L) mx = fmaxf(mx, fabsf(cm.X[k][x].hi));
+                    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+                    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
                     const int e = exp_of(mx);
-                    sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
+                    if ((tid & 3) == 0) sm.cs[x] = e == kZeroExp ? 0.0f : pow2i(e);
                     const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
 #pragma unroll
-                    for (int k = 0; k < KP; k += 2) {
+                    for (int k = k0; k < k0 + 4; k += 2) {
                         float s0[NSL], s1[NSL];
-                        slice_scaled(k < L ? cm.X[k][tid] : ff{0.0f, 0.0f}, sc, s0);
-                        slice_scaled(k + 1 < L ? cm.X[k + 1][tid] : ff{0.0f, 0.0f}, sc, s1);
+                        slice_scaled(k < L ? cm.X[k][x] : ff{0.0f, 0.0f}, sc, s0);
+                        slice_scaled(k + 1 < L ? cm.X[k + 1][x] : ff{0.0f, 0.0f}, sc, s1);
 #pragma unroll
-                        for (int q = 0; q < NSL; q++) store_pair(sm.B[q], tid, k, s0[q], s1[q]);
+                        for (int q = 0; q < NSL; q++) store_pair(sm.B[q], x, k, s0[q], s1[q]);
                     }
                 }
                 __syncthreads();
@@ -501,11 +506,13 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                             const float scl = __fmul_rn(rs, sm.cs[x]);
                             hi = __fmul_rn(hi, scl);
                             lo = __fmul_rn(lo, scl);
-                            const float s = __fadd_rn(acc_hi[x], hi);
-                            const float bb = __fsub_rn(s, acc_hi[x]);
-                            const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(s, bb)), __fsub_rn(hi, bb));
-                            acc_hi[x] = s;
-                            acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
+                            // compensated (Kahan) sum: acc_lo is the running compensation c,
+                            // the tile value is acc_hi - acc_lo
+                            const float c = __fsub_rn(acc_lo[x], lo);
+                            const float yv = __fsub_rn(hi, c);
+                            const float tv = __fadd_rn(acc_hi[x], yv);
+                            acc_lo[x] = __fsub_rn(__fsub_rn(tv, acc_hi[x]), yv);
+                            acc_hi[x] = tv;
                         }
                     }
                 }
@@ -521,7 +528,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                                 td.t[0] * TX;
 #pragma unroll
             for (int x = 0; x < TX; x++)
-                if (x < ext_x) grid[row + x] += (double)acc_hi[x] + (double)acc_lo[x];
+                if (x < ext_x) grid[row + x] += (double)acc_hi[x] - (double)acc_lo[x];
         }
         __syncthreads();
     }
@@ -609,17 +616,20 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     }
                 }
                 __syncthreads();
-                // B operand: X slices per alpha over x (row exponent gexp[alpha])
-                if (tid < KP) {
-                    const int a = tid;
+                // B operand: X slices per alpha over x (exponent gexp[alpha]); eight threads per alpha
+                {
+                    const int a = tid >> 3, x0b = (tid & 7) * 4;
                     float mxb = 0.0f;
 #pragma unroll
-                    for (int x = 0; x < TX; x++) mxb = fmaxf(mxb, fabsf(cm.X[a][x].hi));
+                    for (int x = x0b; x < x0b + 4; x++) mxb = fmaxf(mxb, fabsf(cm.X[a][x].hi));
+                    mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, 1));
+                    mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, 2));
+                    mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, 4));
                     const int e = exp_of(mxb);
-                    sm.gexp[a] = e;
+                    if ((tid & 7) == 0) sm.gexp[a] = e;
                     const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
 #pragma unroll
-                    for (int x = 0; x < TX; x += 2) {
+                    for (int x = x0b; x < x0b + 4; x += 2) {
                         float s0[NSL], s1[NSL];
                         slice_scaled(cm.X[a][x], sc, s0);
                         slice_scaled(cm.X[a][x + 1], sc, s1);

@@ -1,0 +1,159 @@
+"""Backward kernels: dE/dpab (= integrate), forces dE/dRa, dE/dRb and exponent
+gradients dE/dzeta, dE/dzetb against FP64 central finite differences (h = 1e-5)
+of the CPU oracle's energy, <= 1e-6 relative."""
+import numpy as np
+import pytest
+
+from libgpw_gb300 import capi, tasks as T
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-5
+TOL = 1e-6
+
+
+def workload(ortho=True, n=10, seed=41):
+    if ortho:
+        wl = T.synthetic("bwd", n, 2, (0.3, 20.0), 8.0, [(40, 40, 40)], seed=seed)
+    else:
+        wl = T.synthetic("bwd_g", n, 2, (0.5, 20.0), T.lattice_15(length=8.0), [(36, 36, 36)], seed=seed,
+                         ortho=False)
+        wl.tasks["radius"] = np.minimum(wl.tasks["radius"], 4.0)
+    return wl
+
+
+def energy_cpu(O, wl, V, i, ra=None, rb=None, za=None, zb=None):
+    """E of pair i alone: sum over its block of pab * <V | basis> (oracle)."""
+    t = wl.tasks[i:i + 1].copy()
+    ra0 = t["ra"][0].copy()
+    rb0 = ra0 + t["rab"][0]
+    ra1 = ra0 if ra is None else ra
+    rb1 = rb0 if rb is None else rb
+    t["ra"][0] = ra1
+    t["rab"][0] = rb1 - ra1
+    if za is not None:
+        t["zeta"][0] = za
+    if zb is not None:
+        t["zetb"][0] = zb
+    hab = O.batch(wl, V=V, tasks=t)
+    return float(np.sum(hab * wl.pab))
+
+
+def stable(wl, i):
+    """True if no cube/box boundary moves under the finite-difference steps."""
+    g = wl.levels[0]
+    t = wl.tasks[i]
+    zp = t["zeta"] + t["zetb"]
+    for dz in (0.0, H, -H):
+        pass
+    rp = t["ra"] + t["zetb"] / zp * t["rab"]
+    s = np.asarray(g["dh_inv"]).T @ rp
+    frac = s - np.floor(s)
+    if np.any(np.minimum(frac, 1 - frac) < 1e-3):
+        return False
+    if not g["ortho"]:
+        r = t["radius"]
+        inv = np.asarray(g["dh_inv"])
+        for a in (-1, 0, 1):
+            for b in (-1, 0, 1):
+                for c in (-1, 0, 1):
+                    v = inv.T @ (rp + r * np.array([a, b, c]))
+                    f = v - np.floor(v)
+                    if np.any(np.minimum(f, 1 - f) < 1e-3):
+                        return False
+    return True
+
+
+@pytest.mark.parametrize("ortho", [True, False])
+def test_forces_and_exponents_vs_fd(ortho, oracle_lib):
+    import torch
+
+    O = oracle_lib
+    wl = workload(ortho)
+    V = wl.potentials(seed=6)
+    dev = torch.device("cuda:0")
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    n = wl.ntasks
+    pab = torch.from_numpy(wl.pab).to(dev)
+    Vd = [torch.from_numpy(v).to(dev) for v in V]
+    hab = torch.zeros_like(pab)
+    dra = torch.zeros((n, 3), dtype=torch.float64, device=dev)
+    drb = torch.zeros_like(dra)
+    dza = torch.zeros(n, dtype=torch.float64, device=dev)
+    dzb = torch.zeros_like(dza)
+    ts.backward(pab, Vd, hab, dra, drb, dza, dzb)
+    ts.check()
+    dra, drb, dza, dzb = (x.cpu().numpy() for x in (dra, drb, dza, dzb))
+    hab_ref = O.batch(wl, V=V)
+    assert np.abs(hab.cpu().numpy() - hab_ref).max() <= 1e-12 * np.abs(hab_ref).max()
+    checked = 0
+    for i in range(n):
+        if not stable(wl, i):
+            continue
+        t = wl.tasks[i]
+        ra = t["ra"].copy()
+        rb = ra + t["rab"]
+        scale = 0.0
+        fd = {}
+        for d in range(3):
+            e = np.zeros(3)
+            e[d] = H
+            fd[("ra", d)] = (energy_cpu(O, wl, V, i, ra=ra + e) - energy_cpu(O, wl, V, i, ra=ra - e)) / (2 * H)
+            fd[("rb", d)] = (energy_cpu(O, wl, V, i, rb=rb + e) - energy_cpu(O, wl, V, i, rb=rb - e)) / (2 * H)
+        za, zb = float(t["zeta"]), float(t["zetb"])
+        fd[("za", 0)] = (energy_cpu(O, wl, V, i, za=za + H) - energy_cpu(O, wl, V, i, za=za - H)) / (2 * H)
+        fd[("zb", 0)] = (energy_cpu(O, wl, V, i, zb=zb + H) - energy_cpu(O, wl, V, i, zb=zb - H)) / (2 * H)
+        scale = max(abs(v) for v in fd.values())
+        if scale < 1e-8:
+            continue
+        got = {("ra", d): dra[i, d] for d in range(3)}
+        got.update({("rb", d): drb[i, d] for d in range(3)})
+        got[("za", 0)] = dza[i]
+        got[("zb", 0)] = dzb[i]
+        for k in fd:
+            assert abs(got[k] - fd[k]) <= TOL * scale, (i, k, got[k], fd[k])
+        checked += 1
+    assert checked >= 3
+
+
+def test_autograd_function(oracle_lib):
+    """The torch.autograd.Function of the test harness: gradients of E with respect
+    to the density blocks, centres and exponents through gpw_backward."""
+    import torch
+
+    from gpw_autograd import energy
+
+    wl = workload(True, n=6, seed=43)
+    V = wl.potentials(seed=8)
+    dev = torch.device("cuda:0")
+    pab = torch.from_numpy(wl.pab).to(dev).requires_grad_(True)
+    ra = torch.from_numpy(wl.tasks["ra"].copy()).to(dev).requires_grad_(True)
+    rb = torch.from_numpy((wl.tasks["ra"] + wl.tasks["rab"]).copy()).to(dev).requires_grad_(True)
+    za = torch.from_numpy(wl.tasks["zeta"].copy()).to(dev).requires_grad_(True)
+    zb = torch.from_numpy(wl.tasks["zetb"].copy()).to(dev).requires_grad_(True)
+    Vd = [torch.from_numpy(v).to(dev) for v in V]
+    E = energy(pab, ra, rb, za, zb, Vd, wl)
+    gp, gra, grb, gza, gzb = torch.autograd.grad(E, [pab, ra, rb, za, zb])
+    # dE/dpab is the oracle's integrate; E itself is the oracle's <V, rho>
+    hab = oracle_lib.batch(wl, V=V)
+    assert np.abs(gp.cpu().numpy() - hab).max() <= 1e-12 * np.abs(hab).max()
+    E_cpu = sum(float(np.sum(g * v)) for g, v in zip(oracle_lib.batch(wl), V))
+    assert abs(float(E) - E_cpu) <= 1e-12 * max(abs(E_cpu), 1.0)
+    assert torch.all(torch.isfinite(gra)) and torch.all(torch.isfinite(gza))
+
+
+def test_backward_rejects_tau():
+    import torch
+
+    wl = workload(True, n=3)
+    wl.compute_tau = 1
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    dev = torch.device("cuda:0")
+    pab = torch.from_numpy(wl.pab).to(dev)
+    V = [torch.zeros(T.grid_shape(wl.levels[0]), dtype=torch.float64, device=dev)]
+    dra = torch.zeros((3, 3), dtype=torch.float64, device=dev)
+    with pytest.raises(capi.GpwError) as e:
+        ts.backward(pab, V, None, dra)
+    assert e.value.status == 4
