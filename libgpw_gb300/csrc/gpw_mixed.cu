@@ -506,13 +506,13 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                             const float scl = __fmul_rn(rs, sm.cs[x]);
                             hi = __fmul_rn(hi, scl);
                             lo = __fmul_rn(lo, scl);
-                            // compensated (Kahan) sum: acc_lo is the running compensation c,
-                            // the tile value is acc_hi - acc_lo
-                            const float c = __fsub_rn(acc_lo[x], lo);
-                            const float yv = __fsub_rn(hi, c);
-                            const float tv = __fadd_rn(acc_hi[x], yv);
-                            acc_lo[x] = __fsub_rn(__fsub_rn(tv, acc_hi[x]), yv);
-                            acc_hi[x] = tv;
+                            // float-float sum: exact two-sum of the high parts, the
+                            // rounding errors and low parts gathered in acc_lo
+                            const float sv = __fadd_rn(acc_hi[x], hi);
+                            const float bb = __fsub_rn(sv, acc_hi[x]);
+                            const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
+                            acc_hi[x] = sv;
+                            acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
                         }
                     }
                 }
@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                                 td.t[0] * TX;
 #pragma unroll
             for (int x = 0; x < TX; x++)
-                if (x < ext_x) grid[row + x] += (double)acc_hi[x] - (double)acc_lo[x];
+                if (x < ext_x) grid[row + x] += (double)acc_hi[x] + (double)acc_lo[x];
         }
         __syncthreads();
     }
