@@ -67,6 +67,7 @@ struct TPair {
     int64_t coef_off, table_off;
     int o[3];           // cube offset of the tile origin (current image)
     int gx0, gx1;       // tile-local x range inside the cube box
+    ff tc;              // collocate: x of the tile's centre column minus xp (re-expansion point)
 };
 
 struct MixedState {
@@ -237,14 +238,47 @@ __device__ __forceinline__ int pair_index(int L, int b, int a) { return b * L - 
 
 // The pair record is prepared on the host (float-float splits included) and
 // copied word by word; then the packed coefficients.
-__device__ void load_pair(TileCommon &sm, const MixedArgs &A, int task) {
+__device__ __forceinline__ void load_coef(TileCommon &sm, const MixedArgs &A) {
+    const int nc = ncoef(sm.p.lp);
+    for (int t = threadIdx.x; t < nc; t += blockDim.x) sm.coef[t] = A.coef[sm.p.coef_off + t];
+}
+
+__device__ void load_pair(TileCommon &sm, const MixedArgs &A, int task, bool with_coef = true) {
     static_assert(sizeof(TPair) % 4 == 0, "TPair must be word-sized");
     const uint32_t *src = reinterpret_cast<const uint32_t *>(A.pairs + task);
     uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.p);
     for (int t = threadIdx.x; t < (int)(sizeof(TPair) / 4); t += blockDim.x) dst[t] = src[t];
     __syncthreads();
-    const int nc = ncoef(sm.p.lp);
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) sm.coef[t] = A.coef[sm.p.coef_off + t];
+    if (with_coef) load_coef(sm, A);
+}
+
+// Re-expands the x dependence of the coefficients around the tile centre:
+// c'[g][b][a] = sum_{a' >= a} C(a', a) tc^(a' - a) c[g][b][a'], in place (one
+// thread per (g, b) row).  On the tile |x - centre| <= TX h / 2, so the stage-3
+// operands stay well conditioned for the fixed-point slices.
+__device__ void recentre_x(TileCommon &sm) {
+    const int lp = sm.p.lp;
+    const ff tc = sm.p.tc;
+    const int nrow = ((lp + 1) * (lp + 2)) / 2;
+    for (int t = threadIdx.x; t < nrow; t += blockDim.x) {
+        int g = 0, r = t;
+        while (r >= lp + 1 - g) { r -= lp + 1 - g; g++; }
+        const int b = r, amax = lp - g - b;
+        const int base = pidx(lp, g, b, 0);
+        ff c[kNPow];
+#pragma unroll
+        for (int a = 0; a < kNPow; a++) c[a] = a <= amax ? ff{sm.coef[base + a].x, sm.coef[base + a].y} : ff{0.0f, 0.0f};
+        for (int a = 0; a <= amax; a++) {
+            // Horner in tc over a' = amax .. a with weights C(a', a)
+            ff s = {0.0f, 0.0f};
+            for (int ap = amax; ap >= a; ap--) {
+                float bin = 1.0f;  // C(ap, a)
+                for (int q = 0; q < a; q++) bin = bin * (float)(ap - q) / (float)(q + 1);
+                s = ff_fma(s, tc, ff_mul_f(c[ap], rintf(bin)));
+            }
+            sm.coef[base + a] = make_float2(s.hi, s.lo);
+        }
+    }
 }
 
 // images of one axis: cube offsets o such that the tile [tT, tT+ext) maps onto [lb, hi]
@@ -282,12 +316,15 @@ __device__ __forceinline__ void set_image(TPair &p, int ox, int oy, int oz, int 
     p.o[2] = oz;
     p.gx0 = max(0, p.lb[0] - ox);
     p.gx1 = min(ext_x - 1, p.hi[0] - ox);
+    // centre column TX/2: tc = (ox + TX/2) h - roffset
+    p.tc = ff_add(ff_mul_f(p.h[0], (float)(ox + TX / 2)), ff{-p.off[0].hi, -p.off[0].lo});
 }
 
-// tab[k][i] = t^k exp(-zetp t^2), t = g h - off, g = o + i; zero outside the cube
-// box and outside the valid tile extent.
+// tab[k][i] = u^k exp(-zetp t^2), t = g h - off, g = o + i, and u = t or, with
+// recentre, u = (i - TX/2) h (the offset from the tile centre); zero outside the
+// cube box and outside the valid tile extent.
 __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool inside, ff *col, int stride,
-                                            int L) {
+                                            int L, bool recentre = false, int i = 0) {
     if (!inside) {
         for (int k = 0; k < KP; k++) col[k * stride] = ff{0.0f, 0.0f};
         return;
@@ -295,19 +332,20 @@ __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool i
     const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
     const ff a = ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo});
     ff e = ff_exp(a);
+    const ff u = recentre ? ff_mul_f(p.h[d], (float)(i - TX / 2)) : t;
     for (int k = 0; k < KP; k++) {
         col[k * stride] = k < L ? e : ff{0.0f, 0.0f};
-        if (k + 1 < L) e = ff_mul(e, t);
+        if (k + 1 < L) e = ff_mul(e, u);
     }
 }
 
-__device__ void build_tables(TileCommon &sm, const LevelDev &lv, const TileDesc &td) {
+__device__ void build_tables(TileCommon &sm, const LevelDev &lv, const TileDesc &td, bool recentre_x = false) {
     const TPair &p = sm.p;
     const int tid = threadIdx.x;
     if (tid < TX) {
         const int g = p.o[0] + tid;
         const bool in = tid >= p.gx0 && tid <= p.gx1;
-        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L);
+        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L, recentre_x, tid);
     } else if (tid < TX + TY) {
         const int i = tid - TX, g = p.o[1] + i;
         const bool in = i < min(TY, lv.ngrid[1] - td.t[1] * TY) && g >= p.lb[1] && g <= p.hi[1];
@@ -382,7 +420,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
         const int64_t it_end = A.start[tile + 1];
         for (int64_t it = A.start[tile]; it < it_end && !cm.abort; it++) {
-            load_pair(cm, A, A.items[it]);
+            load_pair(cm, A, A.items[it], false);
             if (tid < 3) {
                 const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
                 axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
@@ -397,7 +435,10 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 }
                 __syncthreads();
                 if (cm.p.gx0 > cm.p.gx1) continue;  // uniform: no x overlap
-                build_tables(cm, lv, td);
+                load_coef(cm, A);
+                __syncthreads();
+                recentre_x(cm);
+                build_tables(cm, lv, td, true);
                 __syncthreads();
                 // stage 1: Cxy[z][(b,a)] = sum_g c[g][b][a] Z[g][z]
                 const int npair = (L * (L + 1)) / 2;
