@@ -67,7 +67,8 @@ struct TPair {
     int64_t coef_off, table_off;
     int o[3];           // cube offset of the tile origin (current image)
     int gx0, gx1;       // tile-local x range inside the cube box
-    ff tc;              // collocate: x of the tile's centre column minus xp (re-expansion point)
+    ff tc;              // collocate: x of the re-expansion column minus xp
+    int ic;             // collocate: tile-local re-expansion column
 };
 
 struct MixedState {
@@ -252,10 +253,10 @@ __device__ void load_pair(TileCommon &sm, const MixedArgs &A, int task, bool wit
     if (with_coef) load_coef(sm, A);
 }
 
-// Re-expands the x dependence of the coefficients around the tile centre:
+// Re-expands the x dependence of the coefficients around column ic of the tile:
 // c'[g][b][a] = sum_{a' >= a} C(a', a) tc^(a' - a) c[g][b][a'], in place (one
-// thread per (g, b) row).  On the tile |x - centre| <= TX h / 2, so the stage-3
-// operands stay well conditioned for the fixed-point slices.
+// thread per (g, b) row).  Powers of the small offsets u = x - x_ic keep the
+// stage-3 operands well conditioned for the fixed-point slices.
 __device__ void recentre_x(TileCommon &sm) {
     const int lp = sm.p.lp;
     const ff tc = sm.p.tc;
@@ -316,13 +317,22 @@ __device__ __forceinline__ void set_image(TPair &p, int ox, int oy, int oz, int 
     p.o[2] = oz;
     p.gx0 = max(0, p.lb[0] - ox);
     p.gx1 = min(ext_x - 1, p.hi[0] - ox);
-    // centre column TX/2: tc = (ox + TX/2) h - roffset
-    p.tc = ff_add(ff_mul_f(p.h[0], (float)(ox + TX / 2)), ff{-p.off[0].hi, -p.off[0].lo});
+    // Re-expansion column: start from the column nearest to the product centre and
+    // move toward the tile centre by at most one Gaussian width 1/sqrt(zetp) --
+    // the largest values stay near u = 0, and broad Gaussians get the smallest
+    // |u| over the whole tile.
+    const float hx = p.h[0].hi;
+    int i0 = (int)rintf(p.off[0].hi / hx) - ox;
+    i0 = min(max(i0, p.gx0), max(p.gx0, p.gx1));
+    const float rg = rsqrtf(p.zetp.hi) / hx;
+    const float dc = fminf(fmaxf((float)(TX / 2 - i0), -rg), rg);
+    p.ic = i0 + (int)rintf(dc);
+    p.tc = ff_add(ff_mul_f(p.h[0], (float)(ox + p.ic)), ff{-p.off[0].hi, -p.off[0].lo});
 }
 
 // tab[k][i] = u^k exp(-zetp t^2), t = g h - off, g = o + i, and u = t or, with
-// recentre, u = (i - TX/2) h (the offset from the tile centre); zero outside the
-// cube box and outside the valid tile extent.
+// recentre, u = (i - ic) h (the offset from the re-expansion column); zero outside
+// the cube box and outside the valid tile extent.
 __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool inside, ff *col, int stride,
                                             int L, bool recentre = false, int i = 0) {
     if (!inside) {
@@ -332,7 +342,7 @@ __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool i
     const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
     const ff a = ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo});
     ff e = ff_exp(a);
-    const ff u = recentre ? ff_mul_f(p.h[d], (float)(i - TX / 2)) : t;
+    const ff u = recentre ? ff_mul_f(p.h[d], (float)(i - p.ic)) : t;
     for (int k = 0; k < KP; k++) {
         col[k * stride] = k < L ? e : ff{0.0f, 0.0f};
         if (k + 1 < L) e = ff_mul(e, u);
