@@ -215,6 +215,7 @@ struct TileCommon {
     uint64_t mbar;
     uint32_t tmem;
     int abort;
+    int kmax;  // collocate: K slots of A/B written by the previous pair (zeroed up to here)
 };
 
 struct alignas(128) SmemColl {
@@ -257,6 +258,19 @@ __device__ void load_pair(TileCommon &sm, const MixedArgs &A, int task, bool wit
 // c'[g][b][a] = sum_{a' >= a} C(a', a) tc^(a' - a) c[g][b][a'], in place (one
 // thread per (g, b) row).  Powers of the small offsets u = x - x_ic keep the
 // stage-3 operands well conditioned for the fixed-point slices.
+__constant__ float c_binom[kNPow][kNPow] = {
+    {1},
+    {1, 1},
+    {1, 2, 1},
+    {1, 3, 3, 1},
+    {1, 4, 6, 4, 1},
+    {1, 5, 10, 10, 5, 1},
+    {1, 6, 15, 20, 15, 6, 1},
+    {1, 7, 21, 35, 35, 21, 7, 1},
+    {1, 8, 28, 56, 70, 56, 28, 8, 1},
+    {1, 9, 36, 84, 126, 126, 84, 36, 9, 1},
+    {1, 10, 45, 120, 210, 252, 210, 120, 45, 10, 1}};
+
 __device__ void recentre_x(TileCommon &sm) {
     const int lp = sm.p.lp;
     const ff tc = sm.p.tc;
@@ -272,11 +286,7 @@ __device__ void recentre_x(TileCommon &sm) {
         for (int a = 0; a <= amax; a++) {
             // Horner in tc over a' = amax .. a with weights C(a', a)
             ff s = {0.0f, 0.0f};
-            for (int ap = amax; ap >= a; ap--) {
-                float bin = 1.0f;  // C(ap, a)
-                for (int q = 0; q < a; q++) bin = bin * (float)(ap - q) / (float)(q + 1);
-                s = ff_fma(s, tc, ff_mul_f(c[ap], rintf(bin)));
-            }
+            for (int ap = amax; ap >= a; ap--) s = ff_fma(s, tc, ff_mul_f(c[ap], c_binom[ap][a]));
             sm.coef[base + a] = make_float2(s.hi, s.lo);
         }
     }
@@ -374,6 +384,7 @@ __device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
         tc::mbar_init(&c.mbar, 1);
         tc::fence_mbar_init();
         c.abort = 0;
+        c.kmax = KP;  // operand buffers start uninitialised: write every slot once
     }
     if (threadIdx.x < 32) {
         tc::tmem_alloc(&c.tmem, ncols);
@@ -467,6 +478,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 // B slices: column x over alpha, scaled by 2^(SLB - fx); four threads per column
                 {
                     const int x = tid >> 2, k0 = (tid & 3) * 4;
+                    const bool live = k0 < max(L, cm.kmax);
                     float mx = 0.0f;
 #pragma unroll
                     for (int k = k0; k < k0 + 4; k++)
@@ -477,7 +489,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     if ((tid & 3) == 0) sm.cs[x] = e == kZeroExp ? 0.0f : pow2i(e);
                     const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
 #pragma unroll
-                    for (int k = k0; k < k0 + 4; k += 2) {
+                    for (int k = k0; k < k0 + 4 && live; k += 2) {
                         float s0[NSL], s1[NSL];
                         slice_scaled(k < L ? cm.X[k][x] : ff{0.0f, 0.0f}, sc, s0);
                         slice_scaled(k + 1 < L ? cm.X[k + 1][x] : ff{0.0f, 0.0f}, sc, s1);
@@ -501,8 +513,10 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 const int em = exp_of(mx);
                 {
                     const float sc = em == kZeroExp ? 0.0f : pow2i(SLB - em);
+                    const int kl = cm.kmax;  // K slots that may hold values of an earlier pair
 #pragma unroll
                     for (int k = 0; k < KP; k += 2) {
+                        if (k >= L && k >= kl) break;
                         float s0[NSL], s1[NSL];
                         slice_scaled(k < L && em != kZeroExp ? sm.cxs[k][m] : ff{0.0f, 0.0f}, sc, s0);
                         slice_scaled(k + 1 < L && em != kZeroExp ? sm.cxs[k + 1][m] : ff{0.0f, 0.0f}, sc, s1);
@@ -532,6 +546,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 const bool ok = tc_wait(cm, phase, A.status);
                 phase ^= 1u;
                 if (!ok) break;
+                if (tid == 0) cm.kmax = L;  // read again only after the next barrier
                 // tcgen05.ld is warp-collective: chunk decisions are made per warp
                 if (__any_sync(0xffffffffu, x0 <= x1)) {
                     const float rs = pow2i(max(em - 2 * SLB, -126));
@@ -548,22 +563,19 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                         for (int i = 0; i < 8; i++) {
                             const int x = 8 * c + i;
                             if (x < x0 || x > x1) continue;
-                            const float d2 = __uint_as_float(r2[i]);
+                            // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30); scl * D2 is exact
+                            // (power of two), so an exact two-sum of it into acc_hi and the
+                            // correction terms into acc_lo keep the float-float sum exact
+                            const float scl = __fmul_rn(rs, sm.cs[x]);
                             const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
                                                __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
                                                          __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
-                            float hi = __fadd_rn(d2, corr);
-                            float lo = __fsub_rn(corr, __fsub_rn(hi, d2));
-                            const float scl = __fmul_rn(rs, sm.cs[x]);
-                            hi = __fmul_rn(hi, scl);
-                            lo = __fmul_rn(lo, scl);
-                            // float-float sum: exact two-sum of the high parts, the
-                            // rounding errors and low parts gathered in acc_lo
+                            const float hi = __fmul_rn(__uint_as_float(r2[i]), scl);
                             const float sv = __fadd_rn(acc_hi[x], hi);
                             const float bb = __fsub_rn(sv, acc_hi[x]);
                             const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
                             acc_hi[x] = sv;
-                            acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
+                            acc_lo[x] = __fadd_rn(acc_lo[x], __fmaf_rn(corr, scl, err));
                         }
                     }
                 }
@@ -804,20 +816,32 @@ __global__ void k_coef_to_ff(const double *__restrict__ c, float2 *__restrict__ 
 // ---------------------------------------------------------------------------
 // host: bin the orthorhombic pairs by tile
 namespace {
-void axis_tiles(const LevelDev &lv, int d, const PairGeom &g, int T, std::vector<int> &out) {
+// Tiles one cube axis touches, with the smallest folded offset |f| (f = g <= 0 ?
+// -g : g - 1) of the cube offsets g that land in each tile.
+struct AxisTile {
+    int tile;
+    int fmin;
+};
+void axis_tiles(const LevelDev &lv, int d, const PairGeom &g, int T, std::vector<AxisTile> &out) {
     out.clear();
     const int N = lv.ngrid[d];
     const int nt = (N + T - 1) / T;
-    std::vector<char> seen(nt, 0);
+    std::vector<int> best(nt, INT32_MAX);
     for (int gg = g.lb[d]; gg <= g.hi[d];) {
         int w;
         if (lv.periodic[d]) w = imod(g.cc[d] + gg, lv.npts[d]);
         else w = gg + imod(g.cc[d] + g.lb[d] + lv.lb_grid[d], lv.npts[d]) - g.lb[d];
         if (w < 0 || w >= N) { gg++; continue; }
         const int t = w / T;
-        if (!seen[t]) { seen[t] = 1; out.push_back(t); }
-        gg += std::min(T - (w - t * T), N - w);
+        const int len = std::min(T - (w - t * T), N - w);
+        const int g1 = std::min(gg + len - 1, g.hi[d]);
+        // smallest folded offset over [gg, g1]
+        const int f = (gg <= 1 && g1 >= 0) ? 0 : (g1 < 0 ? -g1 : gg - 1);
+        best[t] = std::min(best[t], f);
+        gg += len;
     }
+    for (int t = 0; t < nt; t++)
+        if (best[t] != INT32_MAX) out.push_back(AxisTile{t, best[t]});
 }
 }  // namespace
 
@@ -844,7 +868,9 @@ int mixed_build(TaskSet &ts, std::string &err) {
     }
     const int ntiles = (int)tiles.size();
     std::vector<int64_t> count(ntiles + 1, 0);
-    std::vector<int> ax, ay, az;
+    std::vector<AxisTile> ax, ay, az;
+    // a pair visits a tile only if some cube point of the tile can be inside its
+    // sphere: folded distance of the tile's nearest offsets <= radius (with margin)
     auto each = [&](auto &&fn) {
         for (int64_t k = 0; k < northo; k++) {
             const PairGeom &g = ts.h_geom[k];
@@ -853,9 +879,22 @@ int mixed_build(TaskSet &ts, std::string &err) {
             axis_tiles(lv, 1, g, TY, ay);
             axis_tiles(lv, 2, g, TZ, az);
             const int base = lvl_first[g.level];
-            for (int c : az)
-                for (int b : ay)
-                    for (int a : ax) fn(base + (c * nty[g.level] + b) * ntx[g.level] + a, (int)k);
+            const double r2 = g.radius * g.radius * (1.0 + 1e-9) + 1e-12;
+            const double hx = lv.dh[0][0], hy = lv.dh[1][1], hz = lv.dh[2][2];
+            const bool table = g.table_off >= 0;  // explicit cube lists: no culling
+            for (const AxisTile &c : az) {
+                const double dz = c.fmin * hz;
+                if (!table && dz * dz > r2) continue;
+                for (const AxisTile &b : ay) {
+                    const double dy = b.fmin * hy;
+                    if (!table && dz * dz + dy * dy > r2) continue;
+                    for (const AxisTile &a : ax) {
+                        const double dx = a.fmin * hx;
+                        if (!table && dz * dz + dy * dy + dx * dx > r2) continue;
+                        fn(base + (c.tile * nty[g.level] + b.tile) * ntx[g.level] + a.tile, (int)k);
+                    }
+                }
+            }
         }
     };
     each([&](int t, int) { count[t + 1]++; });
