@@ -563,19 +563,23 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                         for (int i = 0; i < 8; i++) {
                             const int x = 8 * c + i;
                             if (x < x0 || x > x1) continue;
-                            // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30); scl * D2 is exact
-                            // (power of two), so an exact two-sum of it into acc_hi and the
-                            // correction terms into acc_lo keep the float-float sum exact
-                            const float scl = __fmul_rn(rs, sm.cs[x]);
+                            // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
+                            // lo the exact remainder (fast two-sum), then an exact two-sum into
+                            // acc_hi: acc_lo then only gathers rounding errors and remainders,
+                            // so it stays ~2^-24 below acc_hi however many pairs a point sees
+                            const float d2 = __uint_as_float(r2[i]);
                             const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
                                                __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
                                                          __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
-                            const float hi = __fmul_rn(__uint_as_float(r2[i]), scl);
+                            const float scl = __fmul_rn(rs, sm.cs[x]);
+                            const float h0 = __fadd_rn(d2, corr);
+                            const float hi = __fmul_rn(h0, scl);
+                            const float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
                             const float sv = __fadd_rn(acc_hi[x], hi);
                             const float bb = __fsub_rn(sv, acc_hi[x]);
                             const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
                             acc_hi[x] = sv;
-                            acc_lo[x] = __fadd_rn(acc_lo[x], __fmaf_rn(corr, scl, err));
+                            acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
                         }
                     }
                 }
