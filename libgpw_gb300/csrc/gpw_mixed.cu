@@ -69,6 +69,7 @@ struct TPair {
     int gx0, gx1;       // tile-local x range inside the cube box
     ff tc;              // collocate: x of the re-expansion column minus xp
     int ic;             // collocate: tile-local re-expansion column
+    int sb;             // collocate: x-variable scale 2^sb of the slices (balancing)
 };
 
 struct MixedState {
@@ -338,11 +339,20 @@ __device__ __forceinline__ void set_image(TPair &p, int ox, int oy, int oz, int 
     const float dc = fminf(fmaxf((float)(TX / 2 - i0), -rg), rg);
     p.ic = i0 + (int)rintf(dc);
     p.tc = ff_add(ff_mul_f(p.h[0], (float)(ox + p.ic)), ff{-p.off[0].hi, -p.off[0].lo});
+    // Balance the powers: u -> u / 2^sb with 2^sb ~ the extent that matters on this
+    // tile, min(max |u|, 2 / sqrt(zetp)); the row coefficients take 2^(k sb), so the
+    // product is unchanged and both operands' slices keep their bits where the
+    // values are.
+    const float umax = (float)max(p.ic - p.gx0, p.gx1 - p.ic) * hx;
+    const float ext = fminf(umax, 2.0f * rsqrtf(p.zetp.hi));
+    int e = 0;
+    if (ext > 0.0f) frexpf(ext, &e);
+    p.sb = ext > 0.0f ? min(max(e, -10), 10) : 0;
 }
 
 // tab[k][i] = u^k exp(-zetp t^2), t = g h - off, g = o + i, and u = t or, with
-// recentre, u = (i - ic) h (the offset from the re-expansion column); zero outside
-// the cube box and outside the valid tile extent.
+// recentre, u = (i - ic) h / 2^sb (the balanced offset from the re-expansion
+// column); zero outside the cube box and outside the valid tile extent.
 __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool inside, ff *col, int stride,
                                             int L, bool recentre = false, int i = 0) {
     if (!inside) {
@@ -352,7 +362,7 @@ __device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool i
     const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
     const ff a = ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo});
     ff e = ff_exp(a);
-    const ff u = recentre ? ff_mul_f(p.h[d], (float)(i - p.ic)) : t;
+    const ff u = recentre ? ff_mul_f(p.h[d], ldexpf((float)(i - p.ic), -p.sb)) : t;
     for (int k = 0; k < KP; k++) {
         col[k * stride] = k < L ? e : ff{0.0f, 0.0f};
         if (k + 1 < L) e = ff_mul(e, u);
@@ -506,6 +516,9 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     for (int a = 0; a < L; a++) {
                         ff s = {0.0f, 0.0f};
                         for (int b = 0; b <= lp - a; b++) s = ff_fma(cm.Cxy[z][pair_index(L, b, a)], cm.Y[b][y], s);
+                        const float bal = pow2i(a * cm.p.sb);  // balancing of the x powers
+                        s.hi = __fmul_rn(s.hi, bal);
+                        s.lo = __fmul_rn(s.lo, bal);
                         sm.cxs[a][m] = s;
                         mx = fmaxf(mx, fabsf(s.hi));
                     }
