@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the FP64 error check of the mixed path")
+    ap.add_argument("--no-graph", action="store_true", help="launch the step directly instead of replaying a CUDA graph")
     return ap.parse_args()
 
 
@@ -251,8 +252,21 @@ def main():
         step()
     ts.check()
     torch.cuda.synchronize()
+    # the whole step as one CUDA graph (collocate + integrate: set-up, tiled
+    # kernels, queue resets, back-transform)
+    graph = None
+    if not args.no_graph:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            step()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            step()
+        graph.replay()
+        torch.cuda.synchronize()
     ts.stats()
-    ts.profile(True)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     barrier()
@@ -261,14 +275,25 @@ def main():
         for k in range(args.steps):
             flush.zero_()
             starts[k].record()
-            step()
+            if graph is not None:
+                graph.replay()
+            else:
+                step()
             ends[k].record()
         torch.cuda.synchronize()
     barrier()
     ts.check()
     ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    # per-kernel device time of the same step, measured on one direct step
+    ts.stats()
+    ts.profile(True)
+    flush.zero_()
+    step()
+    torch.cuda.synchronize()
     kern_ms, kern_launches, n_kernels = ts.stats()
     ts.profile(False)
+    kern_ms *= args.steps
+    kern_launches *= args.steps
     if world > 1:
         import torch.distributed as dist
 
@@ -367,8 +392,9 @@ def main():
                    "precision": prec, "compute_tau": wl.compute_tau,
                    "l2": "grid and potential exceed L2; a 512 MB buffer is written between timed steps",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "launch": "CUDA graph replay of the step" if graph is not None else "direct launches",
                    "plan_seconds": plan_s},
-        "gpu_launches": int(n_kernels / max(args.steps, 1) * args.steps),
+        "gpu_launches": int(n_kernels * args.steps),
         "roofline": roof, "error": err, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e,
         "algorithmic_cube_points": points,
     }

@@ -347,6 +347,13 @@ int gpw_plan_create(gpw_plan **plan, int nlevels, const gpw_grid_desc *levels, i
         return cuda_fail(e, "gpw_plan_create");
     }
     P->h_tmat.swap(tm);
+    int smem_max = 0;
+    cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    e = fp64_kernel_attributes(smem_max);
+    if (e != cudaSuccess) {
+        gpw_plan_destroy(P);
+        return cuda_fail(e, "gpw_plan_create (kernel attributes)");
+    }
     *plan = P;
     return GPW_SUCCESS;
 }

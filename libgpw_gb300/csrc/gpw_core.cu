@@ -62,9 +62,11 @@ __global__ void k_integrate_core(int nz, int ny, int nx, int L, const double *__
 cudaError_t launch_collocate_core(const int length[3], int L, const double *co, const double *pol, int ld,
                                   double *out, cudaStream_t s) {
     const int smem = 8 * (L * L + length[1] * L);
-    cudaError_t e = cudaFuncSetAttribute((const void *)k_collocate_core,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute((const void *)k_collocate_core,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+    }
     k_collocate_core<<<length[0], 256, smem, s>>>(length[0], length[1], length[2], L, co, pol, ld, out);
     return cudaGetLastError();
 }

@@ -472,11 +472,22 @@ static cudaError_t set_smem(const void *fn, int bytes) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
+// Opt every dynamic-shared-memory kernel of this file into the device maximum once,
+// so that launches (and CUDA graph capture) need no attribute calls.
+cudaError_t fp64_kernel_attributes(int smem_max) {
+    const void *fns[] = {(const void *)k_prep, (const void *)k_backtransform,
+                         (const void *)k_ortho_fp64<false>, (const void *)k_ortho_fp64<true>,
+                         (const void *)k_general_fp64<false>, (const void *)k_general_fp64<true>};
+    for (const void *fn : fns) {
+        cudaError_t e = set_smem(fn, smem_max);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_prep(const TaskSet &ts, const double *d_pab, cudaStream_t s) {
     if (ts.ntasks == 0) return cudaSuccess;
     const int smem = smem_prep(ts.max_A, ts.max_B);
-    cudaError_t e = set_smem((const void *)k_prep, smem);
-    if (e != cudaSuccess) return e;
     ts.n_kernels++;
     k_prep<<<(unsigned)ts.ntasks, 128, smem, s>>>(ts.d_geom, ts.plan->d_levels, ts.plan->d_tmat,
                                                   ts.tau, d_pab, ts.d_coef);
@@ -494,8 +505,8 @@ static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool a
             fn = adj ? (const void *)k_ortho_fp64<true> : (const void *)k_ortho_fp64<false>;
         else
             fn = adj ? (const void *)k_general_fp64<true> : (const void *)k_general_fp64<false>;
-        cudaError_t e = set_smem(fn, c.smem_bytes);
-        if (e != cudaSuccess) return e;
+        (void)fn;
+        cudaError_t e;
         ProfScope prof(ts, s);
         if (c.kind == 0) {
             if (adj)
@@ -540,8 +551,6 @@ cudaError_t launch_backtransform(const TaskSet &ts, const double *d_mom, double 
                                  cudaStream_t s) {
     if (ts.ntasks == 0) return cudaSuccess;
     const int smem = smem_prep(ts.max_A, ts.max_B);
-    cudaError_t e = set_smem((const void *)k_backtransform, smem);
-    if (e != cudaSuccess) return e;
     ts.n_kernels++;
     k_backtransform<<<(unsigned)ts.ntasks, 128, smem, s>>>(ts.d_geom, ts.plan->d_levels,
                                                            ts.plan->d_tmat, ts.tau, d_mom, d_hab);

@@ -94,6 +94,7 @@ int smem_general_fp64(const PairGeom &g, int extra = 0);
 // moments <V | t^k...> up to degree lp + extra into out (offsets coef_off, or mom_ext_off when extra > 0)
 cudaError_t launch_moments_fp64(const TaskSet &ts, const GridPtrs &g, int extra, double *out, cudaStream_t s);
 int smem_prep(int A, int B);
+cudaError_t fp64_kernel_attributes(int smem_max);
 
 // gpw_core.cu
 cudaError_t launch_collocate_core(const int length[3], int L, const double *co, const double *pol,
