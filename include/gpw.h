@@ -184,6 +184,28 @@ int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
  */
 int gpw_selftest_tensorcore(int64_t *mismatches);
 
+/*
+ * Collocation that allocates no device memory (no counterpart in the
+ * reference).  For callers that cannot allocate on their call path, because
+ * their device memory belongs to their own pool allocator.  Collocates up to
+ * GPW_NOALLOC_MAX_TASKS pairs on one orthorhombic level: d_grid (device,
+ * double[ngrid[2]][ngrid[1]][ngrid[0]]) += rho, with the density blocks in
+ * d_pab (device, addressed as in gpw_task).  Tasks use level 0 and the radius
+ * rule (sphere_offset < 0).  FP64 arithmetic, the plain FP64 kernels.
+ * The scratch (level, pair geometry, coefficients, about 200 KB) is one
+ * fixed device array in the library, held by every GPU that loads it until
+ * the process exits; its device address is looked up on the first call on
+ * each device (make that first call with the device current, and before any
+ * stream capture begins).  All calls
+ * share it: calls that overlap on the GPU (different streams or threads
+ * without ordering) race.  Waits for `stream` before returning.
+ * Larger batches: gpw_taskset_create / gpw_collocate.
+ */
+#define GPW_NOALLOC_MAX_TASKS 64
+int gpw_collocate_noalloc(const gpw_grid_desc *level, const gpw_task *tasks,
+                          int ntasks, int compute_tau, const double *d_pab,
+                          double *d_grid, void *stream);
+
 /* Host-buffer convenience calls (copies inside, synchronous) ------------- */
 int gpw_collocate_host(gpw_taskset *ts, int precision, const double *h_pab,
                        double *const *h_grids);

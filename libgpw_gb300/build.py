@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "libgpw_gb300.so")
-SOURCES = ["gpw_capi.cu", "gpw_fp64.cu", "gpw_core.cu", "gpw_mixed.cu", "gpw_backward.cu", "gpw_selftest.cu"]
+SOURCES = ["gpw_capi.cu", "gpw_fp64.cu", "gpw_core.cu", "gpw_mixed.cu", "gpw_backward.cu", "gpw_selftest.cu", "gpw_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC,-ffp-contract=off",
          "-I" + os.path.join(HERE, "..", "include")]

@@ -66,6 +66,7 @@ def lib():
         "gpw_taskset_profile": ([vp, i32], i32),
         "gpw_taskset_stats": ([vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)], i32),
         "gpw_selftest_tensorcore": ([C.POINTER(i64)], i32),
+        "gpw_collocate_noalloc": ([vp, vp, i32, i32, vp, vp, vp], i32),
         "gpw_collocate_core": ([vp, i32, vp, vp, i32, vp, vp], i32),
         "gpw_integrate_core": ([vp, i32, vp, i32, vp, vp, vp], i32),
     }

@@ -248,6 +248,40 @@ std::map<const gpw_taskset *, HostStage> g_stage;
 
 }  // namespace
 
+namespace gpw {
+// One orthorhombic or general level as the kernels see it (host copy).
+int level_from_desc(const gpw_grid_desc &d, LevelDev &v) {
+    memset(&v, 0, sizeof v);
+    for (int i = 0; i < 3; i++) {
+        v.npts[i] = d.npts[i];
+        v.ngrid[i] = d.ngrid[i];
+        v.lb_grid[i] = d.lb_grid[i];
+        v.periodic[i] = d.periodic[i] ? 1 : 0;
+        if (d.npts[i] < 1 || d.ngrid[i] < 1 || (v.periodic[i] && d.ngrid[i] != d.npts[i]))
+            return fail(GPW_ERR_INVALID_ARG, "grid: npts, ngrid >= 1 and ngrid == npts on periodic axes");
+        for (int j = 0; j < 3; j++) {
+            v.dh[i][j] = d.dh[i][j];
+            v.dh_inv[i][j] = d.dh_inv[i][j];
+        }
+    }
+    v.ortho = d.ortho ? 1 : 0;
+    v.grid_elems = (int64_t)d.ngrid[0] * d.ngrid[1] * d.ngrid[2];
+    v.tmat_off = -1;
+    return GPW_SUCCESS;
+}
+
+// Host geometry of one pair on a single level (the task's level must be 0).
+int host_pair_geom(const gpw_task &t, int idx, const LevelDev &lv, int tau, PairGeom &g) {
+    Plan P;
+    P.nlevels = 1;
+    P.lv[0] = lv;
+    std::vector<int> no_table;
+    return make_geom(t, idx, P, tau, nullptr, 0, g, no_table);
+}
+
+void set_last_error(const std::string &msg) { fail(0, msg); }
+}  // namespace gpw
+
 struct gpw_plan : Plan {};
 struct gpw_taskset : TaskSet {};
 

@@ -539,6 +539,20 @@ cudaError_t launch_moments_fp64(const TaskSet &ts, const GridPtrs &g, int extra,
     return launch_fp64_impl(ts, g, true, -1, extra, out, s);
 }
 
+cudaError_t launch_pairs_fp64(const PairGeom *d_geoms, const LevelDev *d_levels, const double *d_tmat,
+                              double *d_coef, int *d_status, int n, int tau, int max_A, int max_B,
+                              int smem_coll, const double *d_pab, double *d_grid, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_prep<<<(unsigned)n, 128, smem_prep(max_A, max_B), s>>>(d_geoms, d_levels, d_tmat, tau, d_pab, d_coef);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    GridPtrs g;
+    for (int l = 0; l < GPW_MAX_LEVELS; l++) g.p[l] = d_grid;
+    k_ortho_fp64<false><<<(unsigned)n, 256, smem_coll, s>>>(d_geoms, 0, d_levels, nullptr, d_coef, nullptr, g,
+                                                          d_status, 0);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
     return launch_fp64_kind(ts, g, false, -1, s);
 }

@@ -108,6 +108,16 @@ void mixed_free(TaskSet &ts);
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 
+// gpw_capi.cu (host helpers)
+int level_from_desc(const gpw_grid_desc &d, LevelDev &v);
+int host_pair_geom(const gpw_task &t, int idx, const LevelDev &lv, int tau, PairGeom &g);
+void set_last_error(const std::string &msg);
+
+// gpw_fp64.cu: set-up + orthorhombic collocate of n pairs from raw device pointers
+cudaError_t launch_pairs_fp64(const PairGeom *d_geoms, const LevelDev *d_levels, const double *d_tmat,
+                              double *d_coef, int *d_status, int n, int tau, int max_A, int max_B,
+                              int smem_coll, const double *d_pab, double *d_grid, cudaStream_t s);
+
 // gpw_selftest.cu
 int tc_selftest(int64_t *mismatches, std::string &err);
 
