@@ -385,7 +385,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32-split tf32x3 + f64" if prec == "mixed" else "f64",
+        "vs_baseline": None, "dtype": "fp16 fixed-point slices (tcgen05, exact f32 sums) + float-float + f64 grid" if prec == "mixed" else "f64",
         "data": "synthetic (seeded)",
         "config": {"workload": wl.name, "npairs": wl.ntasks,
                    "grids": ["x".join(str(int(v)) for v in l["ngrid"]) for l in wl.levels],

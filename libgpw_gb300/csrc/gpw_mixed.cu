@@ -59,27 +59,48 @@ struct TPair {
     double r2;          // radius^2 (FP64, rule decisions)
     double hz, hy, hx;
     float r2f, hzf, hyf, hxf;
+    float hyinvf, hxinvf;  // 1/hy, 1/hx rounded to float
     ff zetp;
     ff off[3];          // roffset
     ff h[3];
     int lb[3], hi[3], cc[3];
     int kgmin, lp, L;
     int64_t coef_off, table_off;
-    int o[3];           // cube offset of the tile origin (current image)
+};
+// A pair's blob: the record padded to kHdr16 16-byte chunks, then its
+// coefficients as float-float (written by every collocate call), padded to 16 bytes.
+constexpr int kHdr16 = (int)((sizeof(TPair) + 15) / 16);
+constexpr int kCoef16Max = (NCOEF_MAX * (int)sizeof(float2) + 15) / 16;
+
+// the current periodic image of a pair over the tile
+struct ImgState {
+    int o[3];           // cube offset of the tile origin
     int gx0, gx1;       // tile-local x range inside the cube box
     ff tc;              // collocate: x of the re-expansion column minus xp
     int ic;             // collocate: tile-local re-expansion column
     int sb;             // collocate: x-variable scale 2^sb of the slices (balancing)
 };
 
+// Per (tile, pair) item, computed once per task set: the images of the pair's
+// cube over the tile (counts per axis packed as n0 | n1 << 8 | n2 << 16) and the
+// state of the first image.  Items with more than one image (small periodic
+// cells) derive the others in the kernel.
+struct alignas(16) ItemImg {
+    ImgState im;
+    int nimg;
+    int pad_[2];
+};
+static_assert(sizeof(ItemImg) == 48, "ItemImg is three 16-byte chunks");
+
 struct MixedState {
     int ntiles = 0;
     int64_t nitems = 0;
     TileDesc *d_tiles = nullptr;
-    TPair *d_pairs = nullptr;    // per sorted task
-    int64_t *d_start = nullptr;  // ntiles + 1
-    int *d_items = nullptr;      // sorted-task indices per tile
-    float2 *d_coef_ff = nullptr;
+    uint4 *d_blob = nullptr;       // pair blobs of the orthorhombic tasks (sorted order)
+    int64_t *d_blob_off = nullptr; // per task: blob offset in 16-byte chunks
+    int64_t *d_start = nullptr;    // ntiles + 1
+    uint64_t *d_items = nullptr;   // per (tile, pair): blob offset << 16 | chunks
+    ItemImg *d_iimg = nullptr;     // per (tile, pair): images
     int *d_queue = nullptr;      // [0]: collocate, [1]: integrate
     int northo = 0;              // ortho tasks come first in sorted order
     int grid_ctas = 0;    // collocate
@@ -92,13 +113,14 @@ struct MixedState {
 // Sphere rule with an FP32 fast path.  The FP32 estimate decides unless it lies
 // within its error bound of an integer; then the exact FP64 rule (the one the
 // host and the oracle use) decides.
-__device__ __forceinline__ int fast_floor_checked(float rem, float r2f, float h, bool &unsure) {
+__device__ __forceinline__ int fast_floor_checked(float rem, float r2f, float hinv, bool &unsure) {
     const float rc = fmaxf(rem, 0.0f);
-    const float v = __fdiv_rn(sqrtf(rc), h);
+    const float rs = rsqrtf(fmaxf(rc, 1e-30f));
+    const float v = __fmul_rn(__fmul_rn(rc, rs), hinv);  // sqrt(rc) / h, relative error < 2^-21
     const float fl = floorf(v);
-    // error of rem ~ 4 ulp(r2f); of sqrt ~ err/(2 sqrt); plus relative 2^-21
+    // error of rem ~ 4 ulp(r2f); of sqrt ~ err/(2 sqrt); plus relative 2^-19
     const float erem = r2f * 4.8e-7f;
-    const float ev = (rc > erem ? erem / (2.0f * sqrtf(rc)) : sqrtf(erem)) / h + v * 1e-6f + 1e-6f;
+    const float ev = __fmul_rn(erem * 0.5f, rs) * hinv + v * 2e-6f + 1e-6f;
     unsure = (v - fl) <= ev || (fl + 1.0f - v) <= ev || rem <= erem;
     return (int)fl;
 }
@@ -106,7 +128,7 @@ __device__ __forceinline__ int fast_floor_checked(float rem, float r2f, float h,
 __device__ __forceinline__ int row_jmax(const TPair &p, int kf) {
     const float dz = (float)(-kf) * p.hzf;
     bool unsure;
-    int j = fast_floor_checked(__fmaf_rn(-dz, dz, p.r2f), p.r2f, p.hyf, unsure);
+    int j = fast_floor_checked(__fmaf_rn(-dz, dz, p.r2f), p.r2f, p.hyinvf, unsure);
     if (unsure) j = rule_jmax(rule_remk(p.r2, kf, p.hz), p.hy);
     return j;
 }
@@ -114,14 +136,14 @@ __device__ __forceinline__ int row_jmax(const TPair &p, int kf) {
 __device__ __forceinline__ int row_imax(const TPair &p, int kf, int jf) {
     const float dz = (float)(-kf) * p.hzf, dy = (float)(-jf) * p.hyf;
     bool unsure;
-    int i = fast_floor_checked(__fmaf_rn(-dy, dy, __fmaf_rn(-dz, dz, p.r2f)), p.r2f, p.hxf, unsure);
+    int i = fast_floor_checked(__fmaf_rn(-dy, dy, __fmaf_rn(-dz, dz, p.r2f)), p.r2f, p.hxinvf, unsure);
     if (unsure) i = rule_imax(rule_remk(p.r2, kf, p.hz), jf, p.hy, p.hx);
     return i;
 }
 
 // Row (z, y) of the tile: cube-local x range [x0, x1] (empty if x0 > x1).
-__device__ __forceinline__ void row_range(const TPair &p, const int *table, int gz, int gy, int ext_ok,
-                                          int &x0, int &x1) {
+__device__ __forceinline__ void row_range(const TPair &p, const ImgState &q, const int *table, int gz, int gy,
+                                          int ext_ok, int &x0, int &x1) {
     x0 = 1;
     x1 = 0;
     if (!ext_ok || gz < p.lb[2] || gz > p.hi[2] || gy < p.lb[1] || gy > p.hi[1]) return;
@@ -140,8 +162,8 @@ __device__ __forceinline__ void row_range(const TPair &p, const int *table, int 
         imin = T[1 + 2 * (1 - T[0]) + T[2 + 2 * kidx] + (jf - jmin)];
     }
     // cube offsets [imin, 1 - imin] -> tile-local
-    x0 = max(imin - p.o[0], p.gx0);
-    x1 = min(1 - imin - p.o[0], p.gx1);
+    x0 = max(imin - q.o[0], q.gx0);
+    x1 = min(1 - imin - q.o[0], q.gx1);
 }
 
 // UMMA canonical K-major layout, no swizzle: core matrices of 8 rows x 16 bytes
@@ -187,13 +209,13 @@ __device__ __forceinline__ ff combine(float d2, float d3, float d4, float d5, in
 }
 
 struct MixedArgs {
-    const TPair *pairs;
+    const uint4 *blob;        // per pair: record (kHdr16 chunks) then float-float coefficients
     const PairGeom *geoms;
     const LevelDev *levels;
     const TileDesc *tiles;
     const int64_t *start;
-    const int *items;
-    const float2 *coef;
+    const uint64_t *items;    // per (tile, pair): blob offset in 16-byte chunks << 16 | chunks to copy
+    const ItemImg *iimg;      // per (tile, pair): images
     const int *table;
     double *mom;  // integrate: per-pair moments
     GridPtrs grids;
@@ -202,11 +224,21 @@ struct MixedArgs {
     int ntiles;
 };
 
+// one pair as staged in shared memory: the record, then its coefficients
+// (collocate only), in the blob's own layout so that it is copied chunk by chunk
+struct alignas(16) PairBuf {
+    union {
+        TPair p;
+        uint4 hdr_[kHdr16];
+    };
+    float2 coef[2 * kCoef16Max];
+};
+
 // shared state of both tiled kernels
 struct TileCommon {
-    TPair p;
-    float2 coef[NCOEF_MAX];
-    ff X[KP][TX];
+    PairBuf pb[2];  // the current pair and the one being fetched
+    ItemImg ii[2];  // their images over this tile
+    ImgState im;    // images after the first of a multi-image item
     ff Y[KP][TY];
     ff Z[KP][TZ];
     ff Cxy[TZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
@@ -216,13 +248,14 @@ struct TileCommon {
     uint64_t mbar;
     uint32_t tmem;
     int abort;
-    int kmax;  // collocate: K slots of A/B written by the previous pair (zeroed up to here)
+    int kmax;  // collocate: K slots of A written by the previous pair (zeroed up to here)
 };
 
 struct alignas(128) SmemColl {
     __half A[NSL][MROWS * KP];  // Cx slices, M=128 x K=16
     __half B[NSL][TX * KP];     // X slices, N=32 x K=16
-    ff cxs[KP][MROWS];          // stage-2 rows (column m belongs to thread m)
+    ff rc[NCOEF_MAX];           // coefficients re-expanded around the tile's column ic
+    float bin[kNPow][kNPow];    // binomials C(a', a) of the re-expansion
     float cs[TX];               // 2^fx per column (0 for an empty column)
     TileCommon c;
 };
@@ -233,64 +266,42 @@ struct alignas(128) SmemInt {
     __half Vs[NSL][MROWS][TX];     // this tile's V slices, unmasked
     ff S[MROWS][KP];
     int gexp[KP];
+    unsigned char rowlive[MROWS];  // row has cube points in the current image
     TileCommon c;
 };
 
 // pair index of (b, a), b + a <= lp, rows of constant b
 __device__ __forceinline__ int pair_index(int L, int b, int a) { return b * L - (b * (b - 1)) / 2 + a; }
 
-// The pair record is prepared on the host (float-float splits included) and
-// copied word by word; then the packed coefficients.
-__device__ __forceinline__ void load_coef(TileCommon &sm, const MixedArgs &A) {
-    const int nc = ncoef(sm.p.lp);
-    for (int t = threadIdx.x; t < nc; t += blockDim.x) sm.coef[t] = A.coef[sm.p.coef_off + t];
+// packed index of (g, b, 0) in closed form: sum_{z<g} (lp-z+1)(lp-z+2)/2 + sum_{y<b} (lp-g-y+1)
+__device__ __forceinline__ int row_start(int lp, int g, int b) {
+    const int n1 = lp + 1, n2 = lp + 1 - g;
+    const int q = lp - g;
+    return (n1 * (n1 + 1) * (n1 + 2) - n2 * (n2 + 1) * (n2 + 2)) / 6 + b * (q + 1) - (b * (b - 1)) / 2;
 }
 
-__device__ void load_pair(TileCommon &sm, const MixedArgs &A, int task, bool with_coef = true) {
-    static_assert(sizeof(TPair) % 4 == 0, "TPair must be word-sized");
-    const uint32_t *src = reinterpret_cast<const uint32_t *>(A.pairs + task);
-    uint32_t *dst = reinterpret_cast<uint32_t *>(&sm.p);
-    for (int t = threadIdx.x; t < (int)(sizeof(TPair) / 4); t += blockDim.x) dst[t] = src[t];
-    __syncthreads();
-    if (with_coef) load_coef(sm, A);
+// ---- asynchronous record copies (cp.async, 16-byte chunks, L2 only)
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(tc::smem_addr(dst)), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Re-expands the x dependence of the coefficients around column ic of the tile:
-// c'[g][b][a] = sum_{a' >= a} C(a', a) tc^(a' - a) c[g][b][a'], in place (one
-// thread per (g, b) row).  Powers of the small offsets u = x - x_ic keep the
-// stage-3 operands well conditioned for the fixed-point slices.
-__constant__ float c_binom[kNPow][kNPow] = {
-    {1},
-    {1, 1},
-    {1, 2, 1},
-    {1, 3, 3, 1},
-    {1, 4, 6, 4, 1},
-    {1, 5, 10, 10, 5, 1},
-    {1, 6, 15, 20, 15, 6, 1},
-    {1, 7, 21, 35, 35, 21, 7, 1},
-    {1, 8, 28, 56, 70, 56, 28, 8, 1},
-    {1, 9, 36, 84, 126, 126, 84, 36, 9, 1},
-    {1, 10, 45, 120, 210, 252, 210, 120, 45, 10, 1}};
-
-__device__ void recentre_x(TileCommon &sm) {
-    const int lp = sm.p.lp;
-    const ff tc = sm.p.tc;
-    const int nrow = ((lp + 1) * (lp + 2)) / 2;
-    for (int t = threadIdx.x; t < nrow; t += blockDim.x) {
-        int g = 0, r = t;
-        while (r >= lp + 1 - g) { r -= lp + 1 - g; g++; }
-        const int b = r, amax = lp - g - b;
-        const int base = pidx(lp, g, b, 0);
-        ff c[kNPow];
-#pragma unroll
-        for (int a = 0; a < kNPow; a++) c[a] = a <= amax ? ff{sm.coef[base + a].x, sm.coef[base + a].y} : ff{0.0f, 0.0f};
-        for (int a = 0; a <= amax; a++) {
-            // Horner in tc over a' = amax .. a with weights C(a', a)
-            ff s = {0.0f, 0.0f};
-            for (int ap = amax; ap >= a; ap--) s = ff_fma(s, tc, ff_mul_f(c[ap], c_binom[ap][a]));
-            sm.coef[base + a] = make_float2(s.hi, s.lo);
-        }
+// Starts copying item it into buf / ii: the pair's record, its coefficients when
+// with_coef, and the item's images.  Each thread waits for its own copies
+// (cp_async_wait_all) before the barrier after which the buffers are read.
+__device__ __forceinline__ void fetch_pair(PairBuf &buf, ItemImg &ii, const MixedArgs &A, int64_t it, uint64_t item,
+                                           bool with_coef) {
+    const uint4 *src = A.blob + (item >> 16);
+    const int n = with_coef ? min((int)(item & 0xFFFFu), kHdr16 + kCoef16Max) : kHdr16;
+    const uint4 *isrc = reinterpret_cast<const uint4 *>(A.iimg + it);
+    uint4 *dst = buf.hdr_;  // the coefficients follow the record without a gap
+    uint4 *idst = reinterpret_cast<uint4 *>(&ii);
+    for (int t = threadIdx.x; t < n + 3; t += blockDim.x) {
+        if (t < n) cp_async16(dst + t, src + t);
+        else cp_async16(idst + (t - n), isrc + (t - n));
     }
+    cp_async_commit();
 }
 
 // images of one axis: cube offsets o such that the tile [tT, tT+ext) maps onto [lb, hi]
@@ -321,72 +332,145 @@ __device__ void axis_images(const LevelDev &lv, int d, int tt, int T, const TPai
     }
 }
 
-// Per image: tile origin in cube offsets and the x range inside the cube box.
-__device__ __forceinline__ void set_image(TPair &p, int ox, int oy, int oz, int ext_x) {
-    p.o[0] = ox;
-    p.o[1] = oy;
-    p.o[2] = oz;
-    p.gx0 = max(0, p.lb[0] - ox);
-    p.gx1 = min(ext_x - 1, p.hi[0] - ox);
+__device__ __forceinline__ void set_image_x(const TPair &p, ImgState &q, int ox, int ext_x) {
+    q.o[0] = ox;
+    q.gx0 = max(0, p.lb[0] - ox);
+    q.gx1 = min(ext_x - 1, p.hi[0] - ox);
     // Re-expansion column: start from the column nearest to the product centre and
     // move toward the tile centre by at most one Gaussian width 1/sqrt(zetp) --
     // the largest values stay near u = 0, and broad Gaussians get the smallest
     // |u| over the whole tile.
     const float hx = p.h[0].hi;
-    int i0 = (int)rintf(p.off[0].hi / hx) - ox;
-    i0 = min(max(i0, p.gx0), max(p.gx0, p.gx1));
+    int i0 = (int)rintf(__fdividef(p.off[0].hi, hx)) - ox;  // any column is valid: approximate
+    i0 = min(max(i0, q.gx0), max(q.gx0, q.gx1));
     const float rg = rsqrtf(p.zetp.hi) / hx;
     const float dc = fminf(fmaxf((float)(TX / 2 - i0), -rg), rg);
-    p.ic = i0 + (int)rintf(dc);
-    p.tc = ff_add(ff_mul_f(p.h[0], (float)(ox + p.ic)), ff{-p.off[0].hi, -p.off[0].lo});
+    q.ic = i0 + (int)rintf(dc);
+    q.tc = ff_add(ff_mul_f(p.h[0], (float)(ox + q.ic)), ff{-p.off[0].hi, -p.off[0].lo});
     // Balance the powers: u -> u / 2^sb with 2^sb ~ the extent that matters on this
     // tile, min(max |u|, 2 / sqrt(zetp)); the row coefficients take 2^(k sb), so the
     // product is unchanged and both operands' slices keep their bits where the
     // values are.
-    const float umax = (float)max(p.ic - p.gx0, p.gx1 - p.ic) * hx;
+    const float umax = (float)max(q.ic - q.gx0, q.gx1 - q.ic) * hx;
     const float ext = fminf(umax, 2.0f * rsqrtf(p.zetp.hi));
-    int e = 0;
-    if (ext > 0.0f) frexpf(ext, &e);
-    p.sb = ext > 0.0f ? min(max(e, -10), 10) : 0;
+    const int e = ((__float_as_int(ext) >> 23) & 0xff) - 126;  // ext = f 2^e, f in [0.5, 1)
+    q.sb = ext >= 1.1754944e-38f ? min(max(e, -10), 10) : 0;
+}
+__device__ __forceinline__ void set_image(const TPair &p, ImgState &q, int ox, int oy, int oz, int ext_x) {
+    q.o[1] = oy;
+    q.o[2] = oz;
+    set_image_x(p, q, ox, ext_x);
 }
 
-// tab[k][i] = u^k exp(-zetp t^2), t = g h - off, g = o + i, and u = t or, with
-// recentre, u = (i - ic) h / 2^sb (the balanced offset from the re-expansion
-// column); zero outside the cube box and outside the valid tile extent.
-__device__ __forceinline__ void table_entry(const TPair &p, int d, int g, bool inside, ff *col, int stride,
-                                            int L, bool recentre = false, int i = 0) {
-    if (!inside) {
-        for (int k = 0; k < KP; k++) col[k * stride] = ff{0.0f, 0.0f};
-        return;
-    }
-    const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
-    const ff a = ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo});
-    ff e = ff_exp(a);
-    const ff u = recentre ? ff_mul_f(p.h[d], ldexpf((float)(i - p.ic), -p.sb)) : t;
-    for (int k = 0; k < KP; k++) {
-        col[k * stride] = k < L ? e : ff{0.0f, 0.0f};
-        if (k + 1 < L) e = ff_mul(e, u);
-    }
-}
-
-__device__ void build_tables(TileCommon &sm, const LevelDev &lv, const TileDesc &td, bool recentre_x = false) {
-    const TPair &p = sm.p;
+// Threads 0-2 derive the periodic images of one axis each and set the first
+// image; the caller's next barrier publishes them.
+__device__ __forceinline__ void pair_images(TileCommon &sm, const TPair &p, const LevelDev &lv, const TileDesc &td,
+                                            int ext_x, int *status) {
     const int tid = threadIdx.x;
-    if (tid < TX) {
-        const int g = p.o[0] + tid;
-        const bool in = tid >= p.gx0 && tid <= p.gx1;
-        table_entry(p, 0, g, in, &sm.X[0][tid], TX, p.L, recentre_x, tid);
-    } else if (tid < TX + TY) {
-        const int i = tid - TX, g = p.o[1] + i;
-        const bool in = i < min(TY, lv.ngrid[1] - td.t[1] * TY) && g >= p.lb[1] && g <= p.hi[1];
-        table_entry(p, 1, g, in, &sm.Y[0][i], TY, p.L);
-    } else if (tid < TX + TY + TZ) {
-        const int i = tid - TX - TY, g = p.o[2] + i;
-        const bool in = i < min(TZ, lv.ngrid[2] - td.t[2] * TZ) && g >= p.lb[2] && g <= p.hi[2];
-        table_entry(p, 2, g, in, &sm.Z[0][i], TZ, p.L);
+    if (tid < 3) {
+        const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
+        axis_images(lv, tid, td.t[tid], T, p, sm.img[tid], sm.nimg[tid], status);
+        if (sm.nimg[tid] > 0) {
+            if (tid == 0) set_image_x(p, sm.im, sm.img[0][0], ext_x);
+            else sm.im.o[tid] = sm.img[tid][0];
+        }
     }
 }
 
+// tab[k][i] = u^k exp(-zetp t^2), t = g h - off, g = o + i, and u = t or, for x
+// with recentre, u = (i - ic) h / 2^sb (the balanced offset from the
+// re-expansion column); zero outside the cube box, outside the valid tile extent
+// and for k >= L.
+//
+// Y and Z: threads TX .. TX+TY-1 and TX+TY .. TX+TY+TZ-1 (warp 1), into shared
+// memory, one code path with runtime loops.
+__device__ void build_yz(TileCommon &sm, const TPair &p, const ImgState &q, const LevelDev &lv, const TileDesc &td) {
+    const int tid = threadIdx.x;
+    if (tid < TX || tid >= TX + TY + TZ) return;
+    const bool isy = tid < TX + TY;
+    const int d = isy ? 1 : 2, i = isy ? tid - TX : tid - TX - TY, T = isy ? TY : TZ;
+    ff *col = isy ? &sm.Y[0][i] : &sm.Z[0][i];
+    const int g = q.o[d] + i;
+    const bool in = i < min(T, lv.ngrid[d] - td.t[d] * T) && g >= p.lb[d] && g <= p.hi[d];
+    const int L = in ? p.L : 0;
+    if (in) {
+        const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
+        ff e = ff_exp(ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo}));
+#pragma unroll 1
+        for (int k = 0; k < L; k++) {
+            col[k * T] = e;
+            e = ff_mul(e, t);
+        }
+    }
+#pragma unroll 1
+    for (int k = L; k < KP; k++) col[k * T] = ff{0.0f, 0.0f};
+}
+
+// X: column x in registers of one thread (warp 0, x = lane), xv[k] for k < kNPow
+__device__ __forceinline__ void x_column(const TPair &p, const ImgState &q, int x, bool recentre, ff *xv) {
+#pragma unroll
+    for (int k = 0; k < kNPow; k++) xv[k] = ff{0.0f, 0.0f};
+    if (x < q.gx0 || x > q.gx1) return;
+    const ff t = ff_add(ff_mul_f(p.h[0], (float)(q.o[0] + x)), ff{-p.off[0].hi, -p.off[0].lo});
+    ff e = ff_exp(ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo}));
+    const ff u = recentre ? ff_mul_f(p.h[0], ldexpf((float)(x - q.ic), -q.sb)) : t;
+#pragma unroll
+    for (int k = 0; k < kNPow; k++) {
+        if (k >= p.L) break;
+        xv[k] = e;
+        e = ff_mul(e, u);
+    }
+}
+
+// Binomials C(a', a) of the re-expansion c'[g][b][a] = sum_{a' >= a} C(a', a)
+// tc^(a' - a) c[g][b][a'] around column ic of the tile: powers of the small
+// offsets u = x - x_ic keep the stage-3 operands well conditioned for the
+// fixed-point slices.
+__constant__ float c_binom[kNPow][kNPow] = {
+    {1},
+    {1, 1},
+    {1, 2, 1},
+    {1, 3, 3, 1},
+    {1, 4, 6, 4, 1},
+    {1, 5, 10, 10, 5, 1},
+    {1, 6, 15, 20, 15, 6, 1},
+    {1, 7, 21, 35, 35, 21, 7, 1},
+    {1, 8, 28, 56, 70, 56, 28, 8, 1},
+    {1, 9, 36, 84, 126, 126, 84, 36, 9, 1},
+    {1, 10, 45, 120, 210, 252, 210, 120, 45, 10, 1}};
+
+// One item (g, b, a) per thread of [t0, t0 + nt): Horner in tc over a' = amax .. a
+// with the binomials from shared memory (bin[a'][a] = C(a', a)).
+__device__ void recentre_x(const PairBuf &pb, ff tc, ff *out, const float (*bin)[kNPow], int t0, int nt) {
+    const int lp = pb.p.lp;
+    const int nc = ncoef(lp);
+    for (int t = (int)threadIdx.x - t0; t < nc; t += nt) {
+        int g = 0, b = 0, r = t;
+        for (g = 0; g <= lp; g++) {
+            const int cnt = ((lp - g + 1) * (lp - g + 2)) / 2;
+            if (r < cnt) break;
+            r -= cnt;
+        }
+        const int qn = lp - g;
+        for (b = 0; b <= qn; b++) {
+            if (r <= qn - b) break;
+            r -= qn - b + 1;
+        }
+        const int a = r, amax = lp - g - b;
+        const int base = t - a;  // packed index of (g, b, 0)
+        ff s = {0.0f, 0.0f};
+        for (int ap = amax; ap >= a; ap--) {
+            const float2 c = pb.coef[base + ap];
+            s = ff_fma(s, tc, ff_mul_f(ff{c.x, c.y}, bin[ap][a]));
+        }
+        out[t] = s;
+    }
+}
+
+// mask of two packed halves from bits 0 (low half) and 1 (high half) of b
+__device__ __forceinline__ uint32_t half_mask(uint32_t b) {
+    return ((0u - (b & 1u)) & 0x0000FFFFu) | ((0u - ((b >> 1) & 1u)) & 0xFFFF0000u);
+}
 
 // TMEM set-up shared by both kernels: warp 0 allocates, thread 0 inits the mbarrier
 __device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
@@ -407,6 +491,7 @@ __device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
 
 __device__ __forceinline__ void tc_teardown(TileCommon &c, uint32_t ncols, uint32_t phase) {
     if (c.abort) tc::mbar_wait_bounded(&c.mbar, phase, 1u << 22);  // let an MMA in flight finish
+    cp_async_wait_all();
     tc::fence_before_sync();
     __syncthreads();
     if (threadIdx.x < 32) tc::tmem_dealloc(c.tmem, ncols);
@@ -423,10 +508,43 @@ __device__ __forceinline__ bool tc_wait(TileCommon &c, uint32_t phase, int *stat
     return !c.abort;
 }
 
+// The pair loop of a tile: item it + 1 is copied while item it is processed.
+// Returns the buffer slot of item it once it is visible to all threads.
+__device__ __forceinline__ int next_pair(TileCommon &cm, const MixedArgs &A, int64_t it, int64_t it0, int64_t it1,
+                                         uint64_t &nxt, bool with_coef) {
+    const int cur = (int)((it - it0) & 1);
+    cp_async_wait_all();
+    __syncthreads();  // item it visible; every thread is done with the other slot
+    if (it + 1 < it1) {
+        fetch_pair(cm.pb[cur ^ 1], cm.ii[cur ^ 1], A, it + 1, nxt, with_coef);
+        if (it + 2 < it1) nxt = A.items[it + 2];
+    }
+    return cur;
+}
+
+__device__ __forceinline__ void first_pair(TileCommon &cm, const MixedArgs &A, int64_t it0, int64_t it1,
+                                           uint64_t &nxt, bool with_coef) {
+    if (it0 < it1) fetch_pair(cm.pb[0], cm.ii[0], A, it0, A.items[it0], with_coef);
+    if (it0 + 1 < it1) nxt = A.items[it0 + 1];
+}
+
+// images of the current item: 1 for the common case (state precomputed in ii);
+// for more, threads 0-2 derive them here (one extra barrier)
+__device__ __forceinline__ int item_images(TileCommon &cm, const ItemImg &ii, const TPair &P, const LevelDev &lv,
+                                           const TileDesc &td, int ext_x, int *status) {
+    const int np = ii.nimg;
+    const int nimg = (np & 0xff) * ((np >> 8) & 0xff) * ((np >> 16) & 0xff);
+    if (nimg > 1) {
+        pair_images(cm, P, lv, td, ext_x, status);
+        __syncthreads();
+    }
+    return nimg;
+}
+
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
+__global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemColl &sm = *reinterpret_cast<SmemColl *>(smraw);
     TileCommon &cm = sm.c;
@@ -437,6 +555,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t idesc = tc::idesc_f16_f32(MROWS, TX);
     uint32_t phase = 0;
+    for (int t = tid; t < kNPow * kNPow; t += NTHR) sm.bin[t / kNPow][t % kNPow] = c_binom[t / kNPow][t % kNPow];
     for (;;) {
         if (tid == 0) cm.tile = atomicAdd(A.queue, 1);
         __syncthreads();
@@ -449,78 +568,107 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
         for (int x = 0; x < TX; x++) acc_hi[x] = acc_lo[x] = 0.0f;
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
-        const int64_t it_end = A.start[tile + 1];
-        for (int64_t it = A.start[tile]; it < it_end && !cm.abort; it++) {
-            load_pair(cm, A, A.items[it], false);
-            if (tid < 3) {
-                const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
-                axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
-            }
-            __syncthreads();
-            const int L = cm.p.L, lp = cm.p.lp;
-            const int nimg = cm.nimg[0] * cm.nimg[1] * cm.nimg[2];
+        const int64_t it0 = A.start[tile], it1 = A.start[tile + 1];
+        uint64_t nxt = 0;
+        first_pair(cm, A, it0, it1, nxt, true);
+        for (int64_t it = it0; it < it1 && !cm.abort; it++) {
+            const int cur = next_pair(cm, A, it, it0, it1, nxt, true);
+            const PairBuf &pb = cm.pb[cur];
+            const TPair &P = pb.p;
+            const int L = P.L, lp = P.lp;
+            const int nimg = item_images(cm, cm.ii[cur], P, lv, td, ext_x, A.status);
+            const ImgState &Q = nimg == 1 ? cm.ii[cur].im : cm.im;
             for (int im = 0; im < nimg && !cm.abort; im++) {
-                if (tid == 0) {
-                    const int ix = im % cm.nimg[0], iy = (im / cm.nimg[0]) % cm.nimg[1], iz = im / (cm.nimg[0] * cm.nimg[1]);
-                    set_image(cm.p, cm.img[0][ix], cm.img[1][iy], cm.img[2][iz], ext_x);
-                }
-                __syncthreads();
-                if (cm.p.gx0 > cm.p.gx1) continue;  // uniform: no x overlap
-                load_coef(cm, A);
-                __syncthreads();
-                recentre_x(cm);
-                build_tables(cm, lv, td, true);
-                __syncthreads();
-                // stage 1: Cxy[z][(b,a)] = sum_g c[g][b][a] Z[g][z]
-                const int npair = (L * (L + 1)) / 2;
-                for (int t = tid; t < TZ * npair; t += NTHR) {
-                    const int zz = t / npair;
-                    int q = t - zz * npair, b = 0;
-                    while (q >= L - b) { q -= L - b; b++; }
-                    const int a = q;
-                    ff s = {0.0f, 0.0f};
-                    for (int g = 0; g <= lp - a - b; g++) {
-                        const float2 c = cm.coef[pidx(lp, g, b, a)];
-                        s = ff_fma(ff{c.x, c.y}, cm.Z[g][zz], s);
+                if (im > 0) {
+                    if (tid == 0) {
+                        const int ix = im % cm.nimg[0], iy = (im / cm.nimg[0]) % cm.nimg[1],
+                                  iz = im / (cm.nimg[0] * cm.nimg[1]);
+                        set_image(P, cm.im, cm.img[0][ix], cm.img[1][iy], cm.img[2][iz], ext_x);
                     }
-                    cm.Cxy[zz][pair_index(L, b, a)] = s;
+                    __syncthreads();
                 }
-                // B slices: column x over alpha, scaled by 2^(SLB - fx); four threads per column
-                {
-                    const int x = tid >> 2, k0 = (tid & 3) * 4;
-                    const bool live = k0 < max(L, cm.kmax);
+                if (Q.gx0 > Q.gx1) continue;  // uniform: no x overlap
+                // warp 0: X column (lane x) and its B slices, scaled by 2^(SLB - fx); warp 1:
+                // Y and Z tables; warps 2-3: re-expansion of the coefficients
+                if (warp == 0) {
+                    ff xv[kNPow];
+                    x_column(P, Q, tid, true, xv);
                     float mx = 0.0f;
 #pragma unroll
-                    for (int k = k0; k < k0 + 4; k++)
-                        if (k < L) mx = fmaxf(mx, fabsf(cm.X[k][x].hi));
-                    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-                    mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 2));
+                    for (int k = 0; k < kNPow; k++) mx = fmaxf(mx, fabsf(xv[k].hi));
                     const int e = exp_of(mx);
-                    if ((tid & 3) == 0) sm.cs[x] = e == kZeroExp ? 0.0f : pow2i(e);
+                    sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
                     const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
+                    const int kw = max(L, cm.kmax);  // slots beyond L that may hold an earlier pair
 #pragma unroll
-                    for (int k = k0; k < k0 + 4 && live; k += 2) {
+                    for (int k = 0; k < KP; k += 2) {
+                        if (k >= kw) break;
                         float s0[NSL], s1[NSL];
-                        slice_scaled(k < L ? cm.X[k][x] : ff{0.0f, 0.0f}, sc, s0);
-                        slice_scaled(k + 1 < L ? cm.X[k + 1][x] : ff{0.0f, 0.0f}, sc, s1);
+                        slice_scaled(k < kNPow ? xv[k < kNPow ? k : 0] : ff{0.0f, 0.0f}, sc, s0);
+                        slice_scaled(k + 1 < kNPow ? xv[k + 1 < kNPow ? k + 1 : 0] : ff{0.0f, 0.0f}, sc, s1);
 #pragma unroll
-                        for (int q = 0; q < NSL; q++) store_pair(sm.B[q], x, k, s0[q], s1[q]);
+                        for (int q = 0; q < NSL; q++) store_pair(sm.B[q], tid, k, s0[q], s1[q]);
+                    }
+                } else if (warp == 1) {
+                    build_yz(cm, P, Q, lv, td);
+                } else {
+                    recentre_x(pb, Q.tc, sm.rc, sm.bin, 64, NTHR - 64);
+                }
+                __syncthreads();
+                // stage 1: Cxy[z][(b,a)] = sum_g c'[g][b][a] Z[g][z]; one output per thread (16
+                // consecutive threads share (b, a)), two partial sums over even and odd g
+                {
+                    const int npair = (L * (L + 1)) / 2;
+                    for (int t = tid; t < TZ * npair; t += NTHR) {
+                        const int zz = t & (TZ - 1), q = t >> 4;
+                        int b = 0, r = q;
+                        while (r >= L - b) {
+                            r -= L - b;
+                            b++;
+                        }
+                        const int a = r, n = lp - a - b;
+                        int off = row_start(lp, 0, b) + a;  // packed index of (g, b, a)
+                        ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+                        int g = 0;
+                        for (; g + 1 <= n; g += 2) {
+                            const int off1 = off + ((lp - g + 1) * (lp - g + 2)) / 2 - b;
+                            s0 = ff_fma(sm.rc[off], cm.Z[g][zz], s0);
+                            s1 = ff_fma(sm.rc[off1], cm.Z[g + 1][zz], s1);
+                            off = off1 + ((lp - g) * (lp - g + 1)) / 2 - b;
+                        }
+                        if (g <= n) s0 = ff_fma(sm.rc[off], cm.Z[g][zz], s0);
+                        cm.Cxy[zz][q] = ff_add(s0, s1);
                     }
                 }
                 __syncthreads();
-                // stage 2 (this thread's row) + culling + A slices
+                // stage 2 (this thread's row, all a at once) + culling + A slices
                 int x0, x1;
-                row_range(cm.p, A.table, cm.p.o[2] + z, cm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
+                row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
+                ff cx[kNPow];
+#pragma unroll
+                for (int a = 0; a < kNPow; a++) cx[a] = ff{0.0f, 0.0f};
                 float mx = 0.0f;
                 if (x0 <= x1) {
-                    for (int a = 0; a < L; a++) {
-                        ff s = {0.0f, 0.0f};
-                        for (int b = 0; b <= lp - a; b++) s = ff_fma(cm.Cxy[z][pair_index(L, b, a)], cm.Y[b][y], s);
-                        const float bal = pow2i(a * cm.p.sb);  // balancing of the x powers
-                        s.hi = __fmul_rn(s.hi, bal);
-                        s.lo = __fmul_rn(s.lo, bal);
-                        sm.cxs[a][m] = s;
-                        mx = fmaxf(mx, fabsf(s.hi));
+                    // b outer (runtime), a inner unrolled with a warp-uniform exit at lp - b:
+                    // one compact loop body for every lp, up to kNPow independent updates
+                    const ff *crow = cm.Cxy[z];
+                    for (int b = 0; b <= lp; b++) {
+                        const ff yb = cm.Y[b][y];
+                        const ff *row = crow + pair_index(L, b, 0);
+                        const int n = lp - b;
+#pragma unroll
+                        for (int a = 0; a < kNPow; a++) {
+                            if (a > n) break;
+                            cx[a] = ff_fma(row[a], yb, cx[a]);
+                        }
+                    }
+                    const int sb = Q.sb;
+#pragma unroll
+                    for (int a = 0; a < kNPow; a++) {
+                        const float bal = pow2i(a * sb);  // balancing of the x powers (exact)
+                        cx[a].hi = __fmul_rn(cx[a].hi, bal);
+                        cx[a].lo = __fmul_rn(cx[a].lo, bal);
+                        mx = fmaxf(mx, fabsf(cx[a].hi));  // entries a > lp are zero
                     }
                 }
                 const int em = exp_of(mx);
@@ -531,8 +679,10 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     for (int k = 0; k < KP; k += 2) {
                         if (k >= L && k >= kl) break;
                         float s0[NSL], s1[NSL];
-                        slice_scaled(k < L && em != kZeroExp ? sm.cxs[k][m] : ff{0.0f, 0.0f}, sc, s0);
-                        slice_scaled(k + 1 < L && em != kZeroExp ? sm.cxs[k + 1][m] : ff{0.0f, 0.0f}, sc, s1);
+                        const ff v0 = (k < kNPow && k < L) ? cx[k < kNPow ? k : 0] : ff{0.0f, 0.0f};
+                        const ff v1 = (k + 1 < kNPow && k + 1 < L) ? cx[k + 1 < kNPow ? k + 1 : 0] : ff{0.0f, 0.0f};
+                        slice_scaled(v0, sc, s0);
+                        slice_scaled(v1, sc, s1);
 #pragma unroll
                         for (int q = 0; q < NSL; q++) store_pair(sm.A[q], m, k, s0[q], s1[q]);
                     }
@@ -600,6 +750,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 __syncthreads();
             }
         }
+        cp_async_wait_all();
         if (cm.abort) break;
         // flush: grid += tile sum (FP64)
         if (z < ext_z && y < ext_y) {
@@ -615,7 +766,6 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     tc_teardown(cm, kCols, phase);
 }
 
-// ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemInt &sm = *reinterpret_cast<SmemInt *>(smraw);
@@ -627,6 +777,9 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t idesc = tc::idesc_f16_f32(MROWS, KP);
     uint32_t phase = 0;
+    // B rows alpha >= L are never written: start them finite (zero)
+    for (int t = tid; t < (int)(sizeof(sm.B) / sizeof(uint4)); t += NTHR)
+        reinterpret_cast<uint4 *>(&sm.B[0][0][0])[t] = make_uint4(0u, 0u, 0u, 0u);
     for (;;) {
         if (tid == 0) cm.tile = atomicAdd(A.queue, 1);
         __syncthreads();
@@ -661,62 +814,81 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     *reinterpret_cast<__half2 *>(&sm.Vs[q][m][x]) = __floats2half2_rn(s0[q], s1[q]);
             }
         }
-        for (int64_t it = A.start[tile]; it < A.start[tile + 1] && !cm.abort; it++) {
-            load_pair(cm, A, A.items[it]);
-            if (tid < 3) {
-                const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
-                axis_images(lv, tid, td.t[tid], T, cm.p, cm.img[tid], cm.nimg[tid], A.status);
-            }
-            __syncthreads();
-            const int L = cm.p.L, lp = cm.p.lp;
+        bool zero_row[2] = {false, false};  // A rows u, u + 64 hold zeros (warps 2-3)
+        const int64_t it0 = A.start[tile], it1 = A.start[tile + 1];
+        uint64_t nxt = 0;
+        first_pair(cm, A, it0, it1, nxt, false);
+        for (int64_t it = it0; it < it1 && !cm.abort; it++) {
+            const int cur = next_pair(cm, A, it, it0, it1, nxt, false);
+            const TPair &P = cm.pb[cur].p;
+            const int L = P.L, lp = P.lp;
             const int npair = (L * (L + 1)) / 2;
-            const int64_t moff = cm.p.coef_off;
-            const int nimg = cm.nimg[0] * cm.nimg[1] * cm.nimg[2];
+            const int64_t moff = P.coef_off;
+            const int nimg = item_images(cm, cm.ii[cur], P, lv, td, ext_x, A.status);
+            const ImgState &Q = nimg == 1 ? cm.ii[cur].im : cm.im;
             for (int im = 0; im < nimg && !cm.abort; im++) {
-                if (tid == 0) {
-                    const int ix = im % cm.nimg[0], iy = (im / cm.nimg[0]) % cm.nimg[1], iz = im / (cm.nimg[0] * cm.nimg[1]);
-                    set_image(cm.p, cm.img[0][ix], cm.img[1][iy], cm.img[2][iz], ext_x);
-                }
-                __syncthreads();
-                if (cm.p.gx0 > cm.p.gx1) continue;
-                build_tables(cm, lv, td);
-                // A operand: this row's V slices masked to the row's cube range
-                int x0, x1;
-                row_range(cm.p, A.table, cm.p.o[2] + z, cm.p.o[1] + y, z < ext_z && y < ext_y, x0, x1);
-#pragma unroll
-                for (int x = 0; x < TX; x += 2) {
-                    const bool in0 = x >= x0 && x <= x1, in1 = x + 1 >= x0 && x + 1 <= x1;
-                    const int o = umma_off(m, x & 15) >> 1, h = x >> 4;
-#pragma unroll
-                    for (int q = 0; q < NSL; q++) {
-                        __half2 v2 = *reinterpret_cast<const __half2 *>(&sm.Vs[q][m][x]);
-                        if (!in0) v2.x = __float2half_rn(0.0f);
-                        if (!in1) v2.y = __float2half_rn(0.0f);
-                        *reinterpret_cast<__half2 *>(&sm.A[h][q][o]) = v2;
+                if (im > 0) {
+                    if (tid == 0) {
+                        const int ix = im % cm.nimg[0], iy = (im / cm.nimg[0]) % cm.nimg[1],
+                                  iz = im / (cm.nimg[0] * cm.nimg[1]);
+                        set_image(P, cm.im, cm.img[0][ix], cm.img[1][iy], cm.img[2][iz], ext_x);
                     }
+                    __syncthreads();
                 }
-                __syncthreads();
-                // B operand: X slices per alpha over x (exponent gexp[alpha]); eight threads per alpha
-                {
-                    const int a = tid >> 3, x0b = (tid & 7) * 4;
-                    float mxb = 0.0f;
+                if (Q.gx0 > Q.gx1) continue;
+                if (warp == 0) {
+                    // X column (lane x) in registers, then B: row alpha = X[alpha][x] over x,
+                    // scaled by 2^(SLB - gexp[alpha]) (maximum over the warp); rows alpha >= L
+                    // are left as they are (their output columns are not read)
+                    ff xv[kNPow];
+                    x_column(P, Q, tid, false, xv);
 #pragma unroll
-                    for (int x = x0b; x < x0b + 4; x++) mxb = fmaxf(mxb, fabsf(cm.X[a][x].hi));
-                    mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, 1));
-                    mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, 2));
-                    mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, 4));
-                    const int e = exp_of(mxb);
-                    if ((tid & 7) == 0) sm.gexp[a] = e;
-                    const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
+                    for (int a = 0; a < kNPow; a++) {
+                        if (a >= L) break;
+                        float mxb = fabsf(xv[a].hi);
 #pragma unroll
-                    for (int x = x0b; x < x0b + 4; x += 2) {
-                        float s0[NSL], s1[NSL];
-                        slice_scaled(cm.X[a][x], sc, s0);
-                        slice_scaled(cm.X[a][x + 1], sc, s1);
-                        const int o = umma_off(a, x & 15) >> 1, h = x >> 4;
+                        for (int o = 16; o > 0; o >>= 1) mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, o));
+                        const int e = exp_of(mxb);
+                        if (tid == 0) sm.gexp[a] = e;
+                        const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
+                        float sl[NSL];
+                        slice_scaled(xv[a], sc, sl);
+                        const int o = umma_off(a, tid & 15) >> 1, h = tid >> 4;
 #pragma unroll
-                        for (int q = 0; q < NSL; q++)
-                            *reinterpret_cast<__half2 *>(&sm.B[h][q][o]) = __floats2half2_rn(s0[q], s1[q]);
+                        for (int q = 0; q < NSL; q++) sm.B[h][q][o] = __float2half_rn(sl[q]);
+                    }
+                } else if (warp == 1) {
+                    build_yz(cm, P, Q, lv, td);
+                } else {
+                    // A operand: V slices of rows u and u + 64 masked to the rows' cube ranges,
+                    // 16-byte chunks (8 x of one K half); rows already zero stay untouched
+                    const int u = tid - 64;
+#pragma unroll
+                    for (int rr = 0; rr < 2; rr++) {
+                        const int r = u + 64 * rr, rz = r / TY, ry = r % TY;
+                        int x0, x1;
+                        row_range(P, Q, A.table, Q.o[2] + rz, Q.o[1] + ry, rz < ext_z && ry < ext_y, x0, x1);
+                        const uint32_t M =
+                            x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));  // bits x0..x1
+                        sm.rowlive[r] = M != 0u;
+                        if (M == 0u && zero_row[rr]) continue;
+                        zero_row[rr] = M == 0u;
+#pragma unroll
+                        for (int v = 0; v < TX / 8; v++) {
+                            const uint32_t mv = M >> (8 * v);
+                            uint4 mk;
+                            mk.x = half_mask(mv);
+                            mk.y = half_mask(mv >> 2);
+                            mk.z = half_mask(mv >> 4);
+                            mk.w = half_mask(mv >> 6);
+                            const int o16 = (r >> 3) * 16 + (v & 1) * 8 + (r & 7);  // umma_off / 16
+#pragma unroll
+                            for (int q = 0; q < NSL; q++) {
+                                const uint4 val = reinterpret_cast<const uint4 *>(&sm.Vs[q][r][0])[v];
+                                reinterpret_cast<uint4 *>(sm.A[v >> 1][q])[o16] =
+                                    make_uint4(val.x & mk.x, val.y & mk.y, val.z & mk.z, val.w & mk.w);
+                            }
+                        }
                     }
                 }
                 tc::fence_async_smem();
@@ -749,6 +921,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                 const bool ok = tc_wait(cm, phase, A.status);
                 phase ^= 1u;
                 if (!ok) break;
+                const bool live = sm.rowlive[m];
 #pragma unroll
                 for (int c = 0; c < KP / 8; c++) {
                     uint32_t ra[8], rb[8], r3[8], r4[8], r5[8];
@@ -763,7 +936,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     for (int i = 0; i < 8; i++) {
                         const int a = 8 * c + i;
                         ff s = {0.0f, 0.0f};
-                        if (a < L && x0 <= x1) {
+                        if (a < L && live) {
                             const ff d2 = two_sum(__uint_as_float(ra[i]), __uint_as_float(rb[i]));
                             ff t = two_sum(d2.hi, __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f));
                             t.lo = __fadd_rn(t.lo, __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
@@ -817,16 +990,60 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                 __syncthreads();
             }
         }
+        cp_async_wait_all();
         if (cm.abort) break;
     }
     tc_teardown(cm, kCols, phase);
 }
 
-__global__ void k_coef_to_ff(const double *__restrict__ c, float2 *__restrict__ out, int64_t n) {
+// the float-float coefficients of every orthorhombic pair into its blob; one warp per pair
+__global__ void k_coef_to_blob(const double *__restrict__ c, uint4 *blob, const int64_t *__restrict__ off16,
+                               int64_t ntask) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t)gridDim.x * (blockDim.x >> 5);
+    for (int64_t k = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); k < ntask; k += nw) {
+        const TPair *p = reinterpret_cast<const TPair *>(blob + off16[k]);
+        const int64_t src = p->coef_off;
+        const int nc = ncoef(p->lp);
+        float2 *dst = reinterpret_cast<float2 *>(blob + off16[k] + kHdr16);
+        for (int t = lane; t < nc; t += 32) {
+            const double d = c[src + t];
+            const float h = __double2float_rn(d);
+            dst[t] = make_float2(h, __double2float_rn(d - (double)h));
+        }
+    }
+}
+
+// the images of every (tile, pair) item, once per task set; one block per tile
+__global__ void k_item_images(const TileDesc *__restrict__ tiles, const int64_t *__restrict__ start,
+                              const uint64_t *__restrict__ items, const uint4 *__restrict__ blob,
+                              const LevelDev *__restrict__ levels, ItemImg *out, int ntiles, int *status) {
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const TileDesc td = tiles[tile];
+        const LevelDev &lv = levels[td.level];
+        const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
+        for (int64_t it = start[tile] + threadIdx.x; it < start[tile + 1]; it += blockDim.x) {
+            const TPair &p = *reinterpret_cast<const TPair *>(blob + (items[it] >> 16));
+            int img[3][kMaxImages], n[3];
+            axis_images(lv, 0, td.t[0], TX, p, img[0], n[0], status);
+            axis_images(lv, 1, td.t[1], TY, p, img[1], n[1], status);
+            axis_images(lv, 2, td.t[2], TZ, p, img[2], n[2], status);
+            ItemImg r;
+            memset(&r, 0, sizeof r);
+            r.nimg = n[0] | (n[1] << 8) | (n[2] << 16);
+            if (n[0] > 0 && n[1] > 0 && n[2] > 0) set_image(p, r.im, img[0][0], img[1][0], img[2][0], ext_x);
+            out[it] = r;
+        }
+    }
+}
+
+// scatters the records (contiguous on input) to their blob offsets
+__global__ void k_place_records(const uint4 *__restrict__ rec, const int64_t *__restrict__ off16, uint4 *blob,
+                                int64_t ntask) {
+    const int64_t n = ntask * kHdr16;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const double d = c[i];
-        const float h = __double2float_rn(d);
-        out[i] = make_float2(h, __double2float_rn(d - (double)h));
+        const int64_t k = i / kHdr16;
+        blob[off16[k] + (i - k * kHdr16)] = rec[i];
     }
 }
 
@@ -924,9 +1141,18 @@ int mixed_build(TaskSet &ts, std::string &err) {
     std::vector<int64_t> start(ntiles + 1, 0);
     for (int i = 0; i < ntiles; i++) start[i + 1] = start[i] + count[order[i] + 1];
     const int64_t nitems = start[ntiles];
-    std::vector<int> items((size_t)std::max<int64_t>(nitems, 1));
+    // blob layout: per task the record, then its coefficients
+    std::vector<int64_t> off16((size_t)std::max<int64_t>(northo, 1), 0);
+    std::vector<int> len16((size_t)std::max<int64_t>(northo, 1), 0);
+    int64_t nchunks = 0;
+    for (int64_t k = 0; k < northo; k++) {
+        off16[k] = nchunks;
+        len16[k] = kHdr16 + (ncoef(ts.h_geom[k].lp) * (int)sizeof(float2) + 15) / 16;
+        nchunks += len16[k];
+    }
+    std::vector<uint64_t> items((size_t)std::max<int64_t>(nitems, 1));
     std::vector<int64_t> fill(start.begin(), start.end() - 1);
-    each([&](int t, int k) { items[fill[rank[t]]++] = k; });
+    each([&](int t, int k) { items[fill[rank[t]]++] = ((uint64_t)off16[k] << 16) | (uint64_t)len16[k]; });
     std::vector<TileDesc> tiles_sorted(ntiles);
     for (int i = 0; i < ntiles; i++) tiles_sorted[i] = tiles[order[i]];
     M->ntiles = ntiles;
@@ -935,7 +1161,7 @@ int mixed_build(TaskSet &ts, std::string &err) {
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 16));
     };
-    std::vector<TPair> pairs((size_t)std::max<int64_t>(northo, 1));
+    std::vector<uint4> recs((size_t)std::max<int64_t>(northo, 1) * kHdr16);
     auto split = [](double d) {
         const float h = (float)d;
         return ff{h, (float)(d - (double)h)};
@@ -943,7 +1169,7 @@ int mixed_build(TaskSet &ts, std::string &err) {
     for (int64_t k = 0; k < northo; k++) {
         const PairGeom &g = ts.h_geom[k];
         const LevelDev &lv = P.lv[g.level];
-        TPair &p = pairs[k];
+        TPair p;
         memset(&p, 0, sizeof p);
         p.r2 = rmul(g.radius, g.radius);
         p.hx = lv.dh[0][0];
@@ -953,6 +1179,8 @@ int mixed_build(TaskSet &ts, std::string &err) {
         p.hxf = (float)p.hx;
         p.hyf = (float)p.hy;
         p.hzf = (float)p.hz;
+        p.hyinvf = (float)(1.0 / p.hy);
+        p.hxinvf = (float)(1.0 / p.hx);
         p.zetp = split(g.zetp);
         for (int d = 0; d < 3; d++) {
             p.off[d] = split(g.off[d]);
@@ -966,21 +1194,42 @@ int mixed_build(TaskSet &ts, std::string &err) {
         p.L = g.lp + 1;
         p.coef_off = g.coef_off;
         p.table_off = g.table_off;
+        memcpy(&recs[(size_t)k * kHdr16], &p, sizeof p);
     }
-    alloc((void **)&M->d_pairs, sizeof(TPair) * pairs.size());
+    alloc((void **)&M->d_blob, sizeof(uint4) * (size_t)std::max<int64_t>(nchunks, 1));
+    alloc((void **)&M->d_blob_off, sizeof(int64_t) * off16.size());
+    if (e == cudaSuccess) e = cudaMemset(M->d_blob, 0, sizeof(uint4) * (size_t)std::max<int64_t>(nchunks, 1));
     if (e == cudaSuccess)
-        e = cudaMemcpy(M->d_pairs, pairs.data(), sizeof(TPair) * pairs.size(), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(M->d_blob_off, off16.data(), sizeof(int64_t) * off16.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && northo > 0) {
+        uint4 *d_recs = nullptr;
+        e = cudaMalloc(&d_recs, sizeof(uint4) * recs.size());
+        if (e == cudaSuccess) e = cudaMemcpy(d_recs, recs.data(), sizeof(uint4) * recs.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) {
+            k_place_records<<<(unsigned)std::min<int64_t>((northo * kHdr16 + 255) / 256, 8192), 256>>>(
+                d_recs, M->d_blob_off, M->d_blob, northo);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+        cudaFree(d_recs);
+    }
     alloc((void **)&M->d_tiles, sizeof(TileDesc) * ntiles);
     alloc((void **)&M->d_start, sizeof(int64_t) * (ntiles + 1));
-    alloc((void **)&M->d_items, sizeof(int) * items.size());
-    alloc((void **)&M->d_coef_ff, sizeof(float2) * std::max<int64_t>(ts.coef_len, 1));
+    alloc((void **)&M->d_items, sizeof(uint64_t) * items.size());
+    alloc((void **)&M->d_iimg, sizeof(ItemImg) * items.size());
     alloc((void **)&M->d_queue, sizeof(int) * 2);
     if (e == cudaSuccess && ntiles)
         e = cudaMemcpy(M->d_tiles, tiles_sorted.data(), sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(M->d_start, start.data(), sizeof(int64_t) * (ntiles + 1), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nitems)
-        e = cudaMemcpy(M->d_items, items.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice);
+        e = cudaMemcpy(M->d_items, items.data(), sizeof(uint64_t) * nitems, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nitems) {
+        k_item_images<<<std::min(ntiles, 8192), 128>>>(M->d_tiles, M->d_start, M->d_items, M->d_blob, P.d_levels,
+                                                       M->d_iimg, ntiles, ts.d_status);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    }
     if (e != cudaSuccess) {
         err = std::string("mixed_build: ") + cudaGetErrorString(e);
         return GPW_ERR_CUDA;
@@ -1021,10 +1270,11 @@ void mixed_free(TaskSet &ts) {
     MixedState *M = ts.mixed;
     if (!M) return;
     cudaFree(M->d_tiles);
-    cudaFree(M->d_pairs);
+    cudaFree(M->d_blob);
+    cudaFree(M->d_blob_off);
     cudaFree(M->d_start);
     cudaFree(M->d_items);
-    cudaFree(M->d_coef_ff);
+    cudaFree(M->d_iimg);
     cudaFree(M->d_queue);
     delete M;
     ts.mixed = nullptr;
@@ -1033,13 +1283,13 @@ void mixed_free(TaskSet &ts) {
 static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which) {
     const MixedState &M = *ts.mixed;
     MixedArgs a;
-    a.pairs = M.d_pairs;
+    a.blob = M.d_blob;
     a.geoms = ts.d_geom;
     a.levels = ts.plan->d_levels;
     a.tiles = M.d_tiles;
     a.start = M.d_start;
     a.items = M.d_items;
-    a.coef = M.d_coef_ff;
+    a.iimg = M.d_iimg;
     a.table = ts.d_table;
     a.mom = ts.d_mom;
     a.grids = g;
@@ -1058,9 +1308,9 @@ cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
     const MixedState &M = *ts.mixed;
     cudaError_t e = cudaSuccess;
     if (M.northo > 0 && M.ntiles > 0) {
-        const int64_t n = ts.coef_len;
         ts.n_kernels++;
-        k_coef_to_ff<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(ts.d_coef, M.d_coef_ff, n);
+        k_coef_to_blob<<<(unsigned)std::min<int64_t>((M.northo + 7) / 8, 8192), 256, 0, s>>>(ts.d_coef, M.d_blob,
+                                                                                               M.d_blob_off, M.northo);
         if ((e = cudaMemsetAsync(M.d_queue, 0, sizeof(int), s)) != cudaSuccess) return e;
         ProfScope prof(ts, s);
         k_collocate_tiled<<<M.grid_ctas, NTHR, sizeof(SmemColl), s>>>(make_args(ts, g, 0));
