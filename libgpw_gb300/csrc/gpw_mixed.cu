@@ -193,10 +193,6 @@ __device__ __forceinline__ void slice_scaled(ff v, float scale, float *sl) {
         r = __fsub_rn(r, sl[i]);
     }
 }
-// two consecutive K entries (k even) of one operand row as packed halves
-__device__ __forceinline__ void store_pair(__half *base, int r, int k, float a, float b) {
-    *reinterpret_cast<__half2 *>(base + (umma_off(r, k) >> 1)) = __floats2half2_rn(a, b);
-}
 
 // Combine the diagonals D_2..D_5 of one product (weights 1, 2^-10, 2^-20, 2^-30)
 // into float-float and scale by 2^E.
@@ -256,17 +252,18 @@ struct alignas(128) SmemColl {
     __half B[NSL][TX * KP];     // X slices, N=32 x K=16
     ff rc[NCOEF_MAX];           // coefficients re-expanded around the tile's column ic
     float bin[kNPow][kNPow];    // binomials C(a', a) of the re-expansion
-    float cs[TX];               // 2^fx per column (0 for an empty column)
+    alignas(16) float cs[TX];   // 2^fx per column (0 for an empty column)
     TileCommon c;
 };
 
 struct alignas(128) SmemInt {
     __half A[2][NSL][MROWS * KP];  // masked V slices, K halves x in [0,16) and [16,32)
     __half B[2][NSL][KP * KP];     // X' slices, N=16 (alpha) x K=16 per half
-    __half Vs[NSL][MROWS][TX];     // this tile's V slices, unmasked
-    ff S[MROWS][KP];
+    __half Vs[2][NSL][MROWS * KP]; // this tile's V slices, unmasked, in the layout of A
+    ff S[MROWS][KP + 1];  // padded rows: conflict-free row-wise stores
     int gexp[KP];
-    unsigned char rowlive[MROWS];  // row has cube points in the current image
+    alignas(16) float xmax[kNPow][TX + 4];  // |X[alpha][x]| for the per-alpha maxima (padded rows)
+    signed char rx0[MROWS], rx1[MROWS];     // each row's cube x range in the current image
     TileCommon c;
 };
 
@@ -472,6 +469,38 @@ __device__ __forceinline__ uint32_t half_mask(uint32_t b) {
     return ((0u - (b & 1u)) & 0x0000FFFFu) | ((0u - ((b >> 1) & 1u)) & 0xFFFF0000u);
 }
 
+// The NSL slices of one K = 16 operand row (v[k] for k < kNPow, zero beyond),
+// scaled by sc, as 16-byte chunks of 8 K values in the UMMA layout (planes of
+// plane_halves halves); K groups at or beyond kw are left as they are.
+__device__ __forceinline__ void slice_row16(const ff *v, float sc, int kw, __half *plane0, int plane_halves,
+                                            int row) {
+#pragma unroll
+    for (int kg = 0; kg < KP / 8; kg++) {
+        if (8 * kg >= kw) break;
+        uint32_t w[NSL][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const int k = 8 * kg + 2 * i;
+            float s0[NSL], s1[NSL];
+            slice_scaled(k < kNPow ? v[k < kNPow ? k : 0] : ff{0.0f, 0.0f}, sc, s0);
+            slice_scaled(k + 1 < kNPow ? v[k + 1 < kNPow ? k + 1 : 0] : ff{0.0f, 0.0f}, sc, s1);
+#pragma unroll
+            for (int q = 0; q < NSL; q++) {
+                const __half2 h2 = __floats2half2_rn(s0[q], s1[q]);
+                w[q][i] = *reinterpret_cast<const uint32_t *>(&h2);
+            }
+        }
+        const int o16 = (row >> 3) * 16 + kg * 8 + (row & 7);  // umma_off(row, 8 kg) / 16
+#pragma unroll
+        for (int q = 0; q < NSL; q++)
+            reinterpret_cast<uint4 *>(plane0 + q * plane_halves)[o16] = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+    }
+}
+
+// named barrier 1 between producer warps (arrive) and consumer warps (sync)
+__device__ __forceinline__ void bar_arrive1(int n) { asm volatile("bar.arrive 1, %0;" ::"r"(n) : "memory"); }
+__device__ __forceinline__ void bar_sync1(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
+
 // TMEM set-up shared by both kernels: warp 0 allocates, thread 0 inits the mbarrier
 __device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
     if (threadIdx.x == 0) {
@@ -599,16 +628,8 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                     const int e = exp_of(mx);
                     sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
                     const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
-                    const int kw = max(L, cm.kmax);  // slots beyond L that may hold an earlier pair
-#pragma unroll
-                    for (int k = 0; k < KP; k += 2) {
-                        if (k >= kw) break;
-                        float s0[NSL], s1[NSL];
-                        slice_scaled(k < kNPow ? xv[k < kNPow ? k : 0] : ff{0.0f, 0.0f}, sc, s0);
-                        slice_scaled(k + 1 < kNPow ? xv[k + 1 < kNPow ? k + 1 : 0] : ff{0.0f, 0.0f}, sc, s1);
-#pragma unroll
-                        for (int q = 0; q < NSL; q++) store_pair(sm.B[q], tid, k, s0[q], s1[q]);
-                    }
+                    // K slots beyond L may hold an earlier pair's slices: rewritten as zeros
+                    slice_row16(xv, sc, max(L, cm.kmax), sm.B[0], TX * KP, tid);
                 } else if (warp == 1) {
                     build_yz(cm, P, Q, lv, td);
                 } else {
@@ -674,18 +695,9 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                 const int em = exp_of(mx);
                 {
                     const float sc = em == kZeroExp ? 0.0f : pow2i(SLB - em);
-                    const int kl = cm.kmax;  // K slots that may hold values of an earlier pair
-#pragma unroll
-                    for (int k = 0; k < KP; k += 2) {
-                        if (k >= L && k >= kl) break;
-                        float s0[NSL], s1[NSL];
-                        const ff v0 = (k < kNPow && k < L) ? cx[k < kNPow ? k : 0] : ff{0.0f, 0.0f};
-                        const ff v1 = (k + 1 < kNPow && k + 1 < L) ? cx[k + 1 < kNPow ? k + 1 : 0] : ff{0.0f, 0.0f};
-                        slice_scaled(v0, sc, s0);
-                        slice_scaled(v1, sc, s1);
-#pragma unroll
-                        for (int q = 0; q < NSL; q++) store_pair(sm.A[q], m, k, s0[q], s1[q]);
-                    }
+                    // entries a > lp of cx are zero; K slots that may hold an earlier pair's
+                    // values (below kmax) are rewritten
+                    slice_row16(cx, sc, max(L, cm.kmax), sm.A[0], MROWS * KP, m);
                 }
                 // stage 3 on the tensor cores: D_s = sum_{i+j=s} A_i B_j^T
                 tc::fence_async_smem();
@@ -717,6 +729,9 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                     for (int c = 0; c < TX / 8; c++) {
                         if (!__any_sync(0xffffffffu, x0 <= x1 && 8 * c <= x1 && 8 * c + 7 >= x0)) continue;
                         uint32_t r2[8], r3[8], r4[8], r5[8];
+                        const float4 csa = reinterpret_cast<const float4 *>(sm.cs)[2 * c];
+                        const float4 csb = reinterpret_cast<const float4 *>(sm.cs)[2 * c + 1];
+                        const float csv[8] = {csa.x, csa.y, csa.z, csa.w, csb.x, csb.y, csb.z, csb.w};
                         tc::tmem_ld8(tbase + 8 * c, r2);
                         tc::tmem_ld8(tbase + 32 + 8 * c, r3);
                         tc::tmem_ld8(tbase + 64 + 8 * c, r4);
@@ -734,7 +749,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                             const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
                                                __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
                                                          __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
-                            const float scl = __fmul_rn(rs, sm.cs[x]);
+                            const float scl = __fmul_rn(rs, csv[i]);
                             const float h0 = __fadd_rn(d2, corr);
                             const float hi = __fmul_rn(h0, scl);
                             const float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
@@ -805,13 +820,23 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
             vm = exp_of(mx);
             const float sc = vm == kZeroExp ? 0.0f : pow2i(SLB - vm);
 #pragma unroll
-            for (int x = 0; x < TX; x += 2) {
-                float s0[NSL], s1[NSL];
-                slice_scaled(v[x], sc, s0);
-                slice_scaled(v[x + 1], sc, s1);
+            for (int c = 0; c < TX / 8; c++) {  // 8 x per 16-byte chunk of the UMMA layout
+                uint32_t w[NSL][4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    float s0[NSL], s1[NSL];
+                    slice_scaled(v[8 * c + 2 * i], sc, s0);
+                    slice_scaled(v[8 * c + 2 * i + 1], sc, s1);
+#pragma unroll
+                    for (int q = 0; q < NSL; q++) {
+                        const __half2 h2 = __floats2half2_rn(s0[q], s1[q]);
+                        w[q][i] = *reinterpret_cast<const uint32_t *>(&h2);
+                    }
+                }
+                const int o16 = (m >> 3) * 16 + (c & 1) * 8 + (m & 7);  // umma_off / 16
 #pragma unroll
                 for (int q = 0; q < NSL; q++)
-                    *reinterpret_cast<__half2 *>(&sm.Vs[q][m][x]) = __floats2half2_rn(s0[q], s1[q]);
+                    reinterpret_cast<uint4 *>(sm.Vs[c >> 1][q])[o16] = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
             }
         }
         bool zero_row[2] = {false, false};  // A rows u, u + 64 hold zeros (warps 2-3)
@@ -836,20 +861,40 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     __syncthreads();
                 }
                 if (Q.gx0 > Q.gx1) continue;
+                {
+                    // every thread: its row's cube x range, for the A operand of warps 2-3
+                    int x0, x1;
+                    row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
+                    const bool empty = x0 > x1;  // otherwise both lie in [0, TX)
+                    sm.rx0[m] = (signed char)(empty ? 1 : x0);
+                    sm.rx1[m] = (signed char)(empty ? 0 : x1);
+                }
                 if (warp == 0) {
+                    bar_arrive1(NTHR);
                     // X column (lane x) in registers, then B: row alpha = X[alpha][x] over x,
                     // scaled by 2^(SLB - gexp[alpha]) (maximum over the warp); rows alpha >= L
                     // are left as they are (their output columns are not read)
                     ff xv[kNPow];
                     x_column(P, Q, tid, false, xv);
+                    // per-alpha maxima over x through shared memory: lane a < L reduces row a
+#pragma unroll
+                    for (int a = 0; a < kNPow; a++) sm.xmax[a][tid] = fabsf(xv[a].hi);
+                    __syncwarp();
+                    if (tid < L) {
+                        const float4 *row = reinterpret_cast<const float4 *>(sm.xmax[tid]);
+                        float mxb = 0.0f;
+#pragma unroll
+                        for (int j = 0; j < TX / 4; j++) {
+                            const float4 f4 = row[j];
+                            mxb = fmaxf(fmaxf(mxb, fmaxf(f4.x, f4.y)), fmaxf(f4.z, f4.w));
+                        }
+                        sm.gexp[tid] = exp_of(mxb);
+                    }
+                    __syncwarp();
 #pragma unroll
                     for (int a = 0; a < kNPow; a++) {
                         if (a >= L) break;
-                        float mxb = fabsf(xv[a].hi);
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) mxb = fmaxf(mxb, __shfl_xor_sync(0xffffffffu, mxb, o));
-                        const int e = exp_of(mxb);
-                        if (tid == 0) sm.gexp[a] = e;
+                        const int e = sm.gexp[a];
                         const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
                         float sl[NSL];
                         slice_scaled(xv[a], sc, sl);
@@ -858,21 +903,28 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                         for (int q = 0; q < NSL; q++) sm.B[h][q][o] = __float2half_rn(sl[q]);
                     }
                 } else if (warp == 1) {
+                    bar_arrive1(NTHR);
                     build_yz(cm, P, Q, lv, td);
                 } else {
+                    bar_sync1(NTHR);
                     // A operand: V slices of rows u and u + 64 masked to the rows' cube ranges,
                     // 16-byte chunks (8 x of one K half); rows already zero stay untouched
                     const int u = tid - 64;
 #pragma unroll
                     for (int rr = 0; rr < 2; rr++) {
-                        const int r = u + 64 * rr, rz = r / TY, ry = r % TY;
-                        int x0, x1;
-                        row_range(P, Q, A.table, Q.o[2] + rz, Q.o[1] + ry, rz < ext_z && ry < ext_y, x0, x1);
+                        const int r = u + 64 * rr;
+                        const int x0 = sm.rx0[r], x1 = sm.rx1[r];
                         const uint32_t M =
                             x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));  // bits x0..x1
-                        sm.rowlive[r] = M != 0u;
                         if (M == 0u && zero_row[rr]) continue;
                         zero_row[rr] = M == 0u;
+                        uint4 val[TX / 8][NSL];  // all loads first: the stores may not pass them
+#pragma unroll
+                        for (int v = 0; v < TX / 8; v++)
+#pragma unroll
+                            for (int q = 0; q < NSL; q++)
+                                val[v][q] = reinterpret_cast<const uint4 *>(
+                                    sm.Vs[v >> 1][q])[(r >> 3) * 16 + (v & 1) * 8 + (r & 7)];
 #pragma unroll
                         for (int v = 0; v < TX / 8; v++) {
                             const uint32_t mv = M >> (8 * v);
@@ -883,11 +935,10 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                             mk.w = half_mask(mv >> 6);
                             const int o16 = (r >> 3) * 16 + (v & 1) * 8 + (r & 7);  // umma_off / 16
 #pragma unroll
-                            for (int q = 0; q < NSL; q++) {
-                                const uint4 val = reinterpret_cast<const uint4 *>(&sm.Vs[q][r][0])[v];
+                            for (int q = 0; q < NSL; q++)
                                 reinterpret_cast<uint4 *>(sm.A[v >> 1][q])[o16] =
-                                    make_uint4(val.x & mk.x, val.y & mk.y, val.z & mk.z, val.w & mk.w);
-                            }
+                                    make_uint4(val[v][q].x & mk.x, val[v][q].y & mk.y, val[v][q].z & mk.z,
+                                               val[v][q].w & mk.w);
                         }
                     }
                 }
@@ -921,7 +972,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                 const bool ok = tc_wait(cm, phase, A.status);
                 phase ^= 1u;
                 if (!ok) break;
-                const bool live = sm.rowlive[m];
+                const bool live = sm.rx0[m] <= sm.rx1[m];
 #pragma unroll
                 for (int c = 0; c < KP / 8; c++) {
                     uint32_t ra[8], rb[8], r3[8], r4[8], r5[8];
@@ -959,9 +1010,13 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     int q = t % npair, b = 0;
                     while (q >= L - b) { q -= L - b; b++; }
                     const int a = q;
-                    ff s = {0.0f, 0.0f};
-                    for (int yy = 0; yy < TY; yy++) s = ff_fma(sm.S[zz * TY + yy][a], cm.Y[b][yy], s);
-                    cm.Cxy[zz][pair_index(L, b, a)] = s;
+                    ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+#pragma unroll
+                    for (int yy = 0; yy < TY; yy += 2) {
+                        s0 = ff_fma(sm.S[zz * TY + yy][a], cm.Y[b][yy], s0);
+                        s1 = ff_fma(sm.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1], s1);
+                    }
+                    cm.Cxy[zz][pair_index(L, b, a)] = ff_add(s0, s1);
                 }
                 __syncthreads();
                 // stage 1 transposed: W[g][b][a] += sum_z T[z][(b,a)] Z[g][z]
@@ -982,9 +1037,14 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                         }
                         a = r;
                     }
-                    ff s = {0.0f, 0.0f};
+                    ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
                     const int pi = pair_index(L, b, a);
-                    for (int zz = 0; zz < TZ; zz++) s = ff_fma(cm.Cxy[zz][pi], cm.Z[g][zz], s);
+#pragma unroll
+                    for (int zz = 0; zz < TZ; zz += 2) {
+                        s0 = ff_fma(cm.Cxy[zz][pi], cm.Z[g][zz], s0);
+                        s1 = ff_fma(cm.Cxy[zz + 1][pi], cm.Z[g][zz + 1], s1);
+                    }
+                    const ff s = ff_add(s0, s1);
                     if (s.hi != 0.0f) atomicAdd(A.mom + moff + t, (double)s.hi + (double)s.lo);
                 }
                 __syncthreads();
