@@ -238,6 +238,7 @@ struct TileCommon {
     ff Y[KP][TY];
     ff Z[KP][TZ];
     ff Cxy[TZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
+    ff cxy_pad_[4];         // stage-2 reads up to 3 entries past a row
     int tile;
     int img[3][kMaxImages];
     int nimg[3];
@@ -677,10 +678,16 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                         const ff yb = cm.Y[b][y];
                         const ff *row = crow + pair_index(L, b, 0);
                         const int n = lp - b;
+                        // chunks of 4 a: one uniform branch per chunk, selects inside (the
+                        // reads past the row stay inside Cxy and its padding)
 #pragma unroll
-                        for (int a = 0; a < kNPow; a++) {
-                            if (a > n) break;
-                            cx[a] = ff_fma(row[a], yb, cx[a]);
+                        for (int a0 = 0; a0 < kNPow; a0 += 4) {
+                            if (a0 > n) break;
+#pragma unroll
+                            for (int a = a0; a < a0 + 4 && a < kNPow; a++) {
+                                const ff t = ff_fma(row[a], yb, cx[a]);
+                                cx[a] = a <= n ? t : cx[a];
+                            }
                         }
                     }
                     const int sb = Q.sb;
@@ -740,7 +747,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
 #pragma unroll
                         for (int i = 0; i < 8; i++) {
                             const int x = 8 * c + i;
-                            if (x < x0 || x > x1) continue;
+                            const bool in = x >= x0 && x <= x1;  // straight-line code: selects, no branches
                             // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
                             // lo the exact remainder (fast two-sum), then an exact two-sum into
                             // acc_hi: acc_lo then only gathers rounding errors and remainders,
@@ -756,8 +763,8 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                             const float sv = __fadd_rn(acc_hi[x], hi);
                             const float bb = __fsub_rn(sv, acc_hi[x]);
                             const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
-                            acc_hi[x] = sv;
-                            acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
+                            acc_lo[x] = in ? __fadd_rn(acc_lo[x], __fadd_rn(err, lo)) : acc_lo[x];
+                            acc_hi[x] = in ? sv : acc_hi[x];
                         }
                     }
                 }
