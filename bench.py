@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-error", action="store_true", help="skip the FP64 error check of the mixed path")
     ap.add_argument("--no-graph", action="store_true", help="launch the step directly instead of replaying a CUDA graph")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="tile shapes from the autotuner's table or the default, never timed here")
     return ap.parse_args()
 
 
@@ -242,6 +244,14 @@ def main():
             prec = "mixed"
         except capi.GpwError:
             prec = "fp64"
+    # tile shapes of the mixed path: the autotuner's table, else timed once here (before any timed region)
+    tiles, tile_src, tune_s = None, None, 0.0
+    if prec == "mixed":
+        from libgpw_gb300 import autotune
+
+        t0 = time.perf_counter()
+        tiles, tile_src = autotune.apply(ts, pab, tasks=wl.tasks, tune=not args.no_tune)
+        tune_s = time.perf_counter() - t0
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
 
     def step():
@@ -393,7 +403,7 @@ def main():
                    "l2": "grid and potential exceed L2; a 512 MB buffer is written between timed steps",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "launch": "CUDA graph replay of the step" if graph is not None else "direct launches",
-                   "plan_seconds": plan_s},
+                   "plan_seconds": plan_s, "tile_z": tiles, "tile_source": tile_src, "tune_seconds": tune_s},
         "gpu_launches": int(n_kernels * args.steps),
         "roofline": roof, "error": err, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e,
         "algorithmic_cube_points": points,

@@ -177,6 +177,30 @@ int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
                       int64_t *contraction_launches, int64_t *kernel_launches);
 
 /*
+ * Tile shapes of the mixed-precision (tiled) path.  Each orthorhombic level is
+ * cut into tiles of 32 x (128 / tz) x tz grid points (x, y, z), tz = 4, 8 or 16;
+ * the shape sets how many tiles a cube touches and how much per-tile work a pair
+ * costs.  No reference counterpart: the reference has no tiled path; the shapes
+ * change the speed, not the results beyond rounding.
+ *
+ * gpw_taskset_set_tiles takes tz per level (nlevels entries) and re-bins the
+ * task set; gpw_taskset_get_tiles returns the current tz per level.  Both wait
+ * for the device: call them when no launch of this task set is in flight.
+ *
+ * gpw_taskset_autotune times one mixed collocate + integrate of the task set on
+ * `stream` for each candidate tz of each level that holds orthorhombic tasks
+ * (one level at a time, the others at their best so far), keeps the fastest
+ * and writes tz per level to tile_z (may be NULL) and the measured ms to
+ * ms[3 * level + c] for the candidates tz = 16, 8, 4 (-1 where not timed; may
+ * be NULL).  d_pab is a density buffer as for gpw_collocate.  The timed calls
+ * run on scratch grids and matrix elements allocated here; the caller's
+ * buffers are not written.
+ */
+int gpw_taskset_set_tiles(gpw_taskset *ts, const int *tile_z);
+int gpw_taskset_get_tiles(const gpw_taskset *ts, int *tile_z);
+int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, double *ms, void *stream);
+
+/*
  * Tensor-core self test on the current device: one fp16 MMA with FP32
  * accumulation (M=128, N=32, K=16) on integer-valued operands in the operand
  * layout the mixed path uses, compared exactly with the integer products.

@@ -65,6 +65,9 @@ def lib():
                                                                                 i32, i32, vp, vp], i32),
         "gpw_taskset_profile": ([vp, i32], i32),
         "gpw_taskset_stats": ([vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)], i32),
+        "gpw_taskset_set_tiles": ([vp, vp], i32),
+        "gpw_taskset_get_tiles": ([vp, vp], i32),
+        "gpw_taskset_autotune": ([vp, vp, vp, vp, vp], i32),
         "gpw_selftest_tensorcore": ([C.POINTER(i64)], i32),
         "gpw_collocate_noalloc": ([vp, vp, i32, i32, vp, vp, vp], i32),
         "gpw_collocate_core": ([vp, i32, vp, vp, i32, vp, vp], i32),
@@ -198,6 +201,27 @@ class TaskSet:
 
     def check(self, stream=None):
         check(lib().gpw_taskset_check(self.handle, _stream_handle(stream)), "device status")
+
+    # tile shapes of the mixed path (z extent per level: 4, 8 or 16)
+    def set_tiles(self, tile_z):
+        tz = np.ascontiguousarray(np.asarray(tile_z, dtype=np.int32).reshape(-1))
+        assert tz.size == len(self.plan.levels)
+        check(lib().gpw_taskset_set_tiles(self.handle, tz.ctypes.data), "gpw_taskset_set_tiles")
+
+    def tiles(self) -> list:
+        tz = np.zeros(len(self.plan.levels), np.int32)
+        check(lib().gpw_taskset_get_tiles(self.handle, tz.ctypes.data), "gpw_taskset_get_tiles")
+        return [int(v) for v in tz]
+
+    def autotune(self, pab, stream=None) -> tuple:
+        """Times each tile shape (gpw_taskset_autotune) and keeps the fastest:
+        (tile z per level, ms[level][candidate tz = 16, 8, 4])."""
+        nl = len(self.plan.levels)
+        tz = np.zeros(nl, np.int32)
+        ms = np.zeros(3 * nl, np.float64)
+        check(lib().gpw_taskset_autotune(self.handle, pab.data_ptr(), tz.ctypes.data, ms.ctypes.data,
+                                         _stream_handle(stream)), "gpw_taskset_autotune")
+        return [int(v) for v in tz], ms.reshape(nl, 3)
 
     # host-buffer calls (numpy in, numpy out; copies inside the library)
     def collocate_host(self, pab: np.ndarray, grids: list, precision: str = "fp64"):

@@ -431,6 +431,7 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
     });
     gpw_taskset *T = new gpw_taskset();
     T->plan = plan;
+    for (int l = 0; l < GPW_MAX_LEVELS; l++) T->tile_lz[l] = kDefaultTileLz;
     T->tau = compute_tau ? 1 : 0;
     T->ntasks = ntasks;
     T->pab_extent = extent;
@@ -601,6 +602,99 @@ int gpw_taskset_check(gpw_taskset *ts, void *stream) {
     if (h & kStatTooManyImages)
         return fail(GPW_ERR_UNSUPPORTED, "a cube spans more periodic images than the tiled path handles");
     return GPW_SUCCESS;
+}
+
+static int tile_lz_of(int tz) { return tz == 4 ? 2 : tz == 8 ? 3 : tz == 16 ? 4 : -1; }
+
+static int retile(gpw_taskset *ts, const int *lz) {
+    bool same = true;
+    for (int l = 0; l < ts->plan->nlevels; l++) same = same && ts->tile_lz[l] == lz[l];
+    if (same && ts->mixed) return GPW_SUCCESS;
+    GPW_CUDA(cudaSetDevice(ts->plan->device));
+    GPW_CUDA(cudaDeviceSynchronize());  // the binned state may be in use by earlier launches
+    mixed_free(*ts);
+    for (int l = 0; l < ts->plan->nlevels; l++) ts->tile_lz[l] = lz[l];
+    std::string err;
+    const int st = mixed_build(*ts, err);
+    if (st) mixed_free(*ts);  // mixed calls then report GPW_ERR_UNSUPPORTED
+    return st ? fail(st, err) : GPW_SUCCESS;
+}
+
+int gpw_taskset_set_tiles(gpw_taskset *ts, const int *tile_z) {
+    if (!ts || !tile_z) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_set_tiles: null");
+    int lz[GPW_MAX_LEVELS];
+    for (int l = 0; l < ts->plan->nlevels; l++) {
+        lz[l] = tile_lz_of(tile_z[l]);
+        if (lz[l] < 0) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_set_tiles: tile z extent must be 4, 8 or 16");
+    }
+    return retile(ts, lz);
+}
+
+int gpw_taskset_get_tiles(const gpw_taskset *ts, int *tile_z) {
+    if (!ts || !tile_z) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_get_tiles: null");
+    for (int l = 0; l < ts->plan->nlevels; l++) tile_z[l] = 1 << ts->tile_lz[l];
+    return GPW_SUCCESS;
+}
+
+int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, double *ms, void *stream) {
+    if (!ts || (ts->ntasks > 0 && !d_pab)) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_autotune: null");
+    const Plan &P = *ts->plan;
+    GPW_CUDA(cudaSetDevice(P.device));
+    cudaStream_t s = (cudaStream_t)stream;
+    // scratch grids (collocate output, then the integrate input) and matrix elements
+    double *grids[GPW_MAX_LEVELS] = {nullptr};
+    double *hab = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t ce = cudaMalloc(&hab, sizeof(double) * (size_t)std::max<int64_t>(ts->pab_extent, 1));
+    for (int l = 0; l < P.nlevels && ce == cudaSuccess; l++) {
+        ce = cudaMalloc(&grids[l], sizeof(double) * P.lv[l].grid_elems);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(grids[l], 0, sizeof(double) * P.lv[l].grid_elems, s);
+    }
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+    if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+    int st = ce == cudaSuccess ? GPW_SUCCESS : cuda_fail(ce, "gpw_taskset_autotune");
+    static const int cand[3] = {4, 3, 2};  // TZ = 16, 8, 4
+    int best[GPW_MAX_LEVELS];
+    for (int l = 0; l < P.nlevels; l++) best[l] = ts->tile_lz[l];
+    auto time_once = [&](float &out) -> int {
+        // one warm-up and one timed collocate + integrate
+        for (int rep = 0; rep < 2; rep++) {
+            if (rep == 1 && (ce = cudaEventRecord(e0, s)) != cudaSuccess) return cuda_fail(ce, "autotune");
+            int r = gpw_collocate(ts, GPW_PREC_MIXED, d_pab, grids, stream);
+            if (!r) r = gpw_integrate(ts, GPW_PREC_MIXED, grids, hab, stream);
+            if (r) return r;
+        }
+        if ((ce = cudaEventRecord(e1, s)) != cudaSuccess || (ce = cudaEventSynchronize(e1)) != cudaSuccess ||
+            (ce = cudaEventElapsedTime(&out, e0, e1)) != cudaSuccess)
+            return cuda_fail(ce, "autotune");
+        return GPW_SUCCESS;
+    };
+    for (int l = 0; l < P.nlevels && !st; l++) {
+        bool used = false;  // levels without orthorhombic tasks keep their shape
+        for (int64_t k = 0; k < ts->ntasks && !used; k++) used = ts->h_geom[k].ortho && ts->h_geom[k].level == l;
+        float best_ms = -1.0f;
+        for (int c = 0; c < 3 && !st; c++) {
+            float t = 0.0f;
+            if (used) {
+                int lz[GPW_MAX_LEVELS];
+                for (int j = 0; j < P.nlevels; j++) lz[j] = best[j];
+                lz[l] = cand[c];
+                st = retile(ts, lz);
+                if (!st) st = time_once(t);
+                if (!st && (best_ms < 0.0f || t < best_ms)) best_ms = t, best[l] = cand[c];
+            }
+            if (ms) ms[3 * l + c] = used ? (double)t : -1.0;
+        }
+    }
+    if (!st) st = retile(ts, best);
+    if (!st) st = gpw_taskset_check(ts, stream);
+    if (tile_z)
+        for (int l = 0; l < P.nlevels; l++) tile_z[l] = 1 << ts->tile_lz[l];
+    for (int l = 0; l < P.nlevels; l++) cudaFree(grids[l]);
+    cudaFree(hab);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return st;
 }
 
 int gpw_taskset_profile(gpw_taskset *ts, int enable) {

@@ -32,6 +32,7 @@ struct Plan {
 };
 
 struct MixedState;  // tiled path, gpw_mixed.cu
+constexpr int kDefaultTileLz = 3;  // tiles of 32 x 16 x 8 points until set or tuned
 
 struct TaskSet {
     Plan *plan = nullptr;
@@ -51,6 +52,7 @@ struct TaskSet {
     int *d_status = nullptr;
     std::vector<Chunk> chunks;     // FP64 launches
     MixedState *mixed = nullptr;
+    int tile_lz[GPW_MAX_LEVELS];   // tiled path: log2 of the tile's z extent per level
     // profiling (gpw_taskset_profile / gpw_taskset_stats)
     bool profile = false;
     mutable std::vector<cudaEvent_t> ev_pool;

@@ -1,6 +1,7 @@
 // Tiled mixed-precision collocate / integrate.
 //
-// Each CTA owns one tile of one grid level (TX x TY x TZ points, x fastest) and
+// Each CTA owns one tile of one grid level (TX x TY x TZ points, x fastest; TX = 32,
+// TY x TZ = 128 rows with TZ = 4, 8 or 16 per level, chosen by the tile autotuner) and
 // walks every pair whose cube touches the tile.  Per pair and tile:
 //   1-D tables t^k exp(-zetp t^2) over the tile's three ranges   (float-float)
 //   stage 1  Cxy[z][b][a] = sum_g c[g][b][a] Z[g][z]              (float-float)
@@ -37,8 +38,9 @@
 
 namespace gpw {
 
-constexpr int TX = 32, TY = 8, TZ = 16;
-constexpr int MROWS = TY * TZ;  // 128 rows per tile, one per thread
+constexpr int TX = 32;
+constexpr int MROWS = 128;       // TY * TZ rows per tile, one per thread
+constexpr int kMaxTY = 32, kMaxTZ = 16;
 constexpr int NTHR = MROWS;
 constexpr int NSL = 4;          // slices per operand
 constexpr int SLB = 10;         // bits per slice
@@ -51,6 +53,13 @@ constexpr int kMaxImages = 4;  // periodic images of one cube axis over one tile
 struct TileDesc {
     int level;
     int t[3];  // tile indices
+    int lz;    // log2 TZ (TY = MROWS >> lz)
+};
+
+// tile extents of a tile descriptor
+struct TileShape {
+    int TY, TZ, ly, lz;
+    __host__ __device__ explicit TileShape(int lz_) : TY(MROWS >> lz_), TZ(1 << lz_), ly(7 - lz_), lz(lz_) {}
 };
 
 // ---------------------------------------------------------------------------
@@ -235,9 +244,9 @@ struct TileCommon {
     PairBuf pb[2];  // the current pair and the one being fetched
     ItemImg ii[2];  // their images over this tile
     ImgState im;    // images after the first of a multi-image item
-    ff Y[KP][TY];
-    ff Z[KP][TZ];
-    ff Cxy[TZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
+    ff Y[KP][kMaxTY];
+    ff Z[KP][kMaxTZ];
+    ff Cxy[kMaxTZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
     ff cxy_pad_[4];         // stage-2 reads up to 3 entries past a row
     int tile;
     int img[3][kMaxImages];
@@ -366,7 +375,8 @@ __device__ __forceinline__ void pair_images(TileCommon &sm, const TPair &p, cons
                                             int ext_x, int *status) {
     const int tid = threadIdx.x;
     if (tid < 3) {
-        const int T = tid == 0 ? TX : (tid == 1 ? TY : TZ);
+        const TileShape sh(td.lz);
+        const int T = tid == 0 ? TX : (tid == 1 ? sh.TY : sh.TZ);
         axis_images(lv, tid, td.t[tid], T, p, sm.img[tid], sm.nimg[tid], status);
         if (sm.nimg[tid] > 0) {
             if (tid == 0) set_image_x(p, sm.im, sm.img[0][0], ext_x);
@@ -380,28 +390,31 @@ __device__ __forceinline__ void pair_images(TileCommon &sm, const TPair &p, cons
 // re-expansion column); zero outside the cube box, outside the valid tile extent
 // and for k >= L.
 //
-// Y and Z: threads TX .. TX+TY-1 and TX+TY .. TX+TY+TZ-1 (warp 1), into shared
-// memory, one code path with runtime loops.
+// Y and Z: entries 0 .. TY-1 and TY .. TY+TZ-1 over the lanes of warp 1, into
+// shared memory, one code path with runtime loops.
 __device__ void build_yz(TileCommon &sm, const TPair &p, const ImgState &q, const LevelDev &lv, const TileDesc &td) {
-    const int tid = threadIdx.x;
-    if (tid < TX || tid >= TX + TY + TZ) return;
-    const bool isy = tid < TX + TY;
-    const int d = isy ? 1 : 2, i = isy ? tid - TX : tid - TX - TY, T = isy ? TY : TZ;
-    ff *col = isy ? &sm.Y[0][i] : &sm.Z[0][i];
-    const int g = q.o[d] + i;
-    const bool in = i < min(T, lv.ngrid[d] - td.t[d] * T) && g >= p.lb[d] && g <= p.hi[d];
-    const int L = in ? p.L : 0;
-    if (in) {
-        const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
-        ff e = ff_exp(ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo}));
+    const TileShape sh(td.lz);
 #pragma unroll 1
-        for (int k = 0; k < L; k++) {
-            col[k * T] = e;
-            e = ff_mul(e, t);
+    for (int ent = (int)threadIdx.x - 32; ent < sh.TY + sh.TZ; ent += 32) {
+        const bool isy = ent < sh.TY;
+        const int d = isy ? 1 : 2, i = isy ? ent : ent - sh.TY, T = isy ? sh.TY : sh.TZ;
+        const int stride = isy ? kMaxTY : kMaxTZ;
+        ff *col = isy ? &sm.Y[0][i] : &sm.Z[0][i];
+        const int g = q.o[d] + i;
+        const bool in = i < min(T, lv.ngrid[d] - td.t[d] * T) && g >= p.lb[d] && g <= p.hi[d];
+        const int L = in ? p.L : 0;
+        if (in) {
+            const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
+            ff e = ff_exp(ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo}));
+#pragma unroll 1
+            for (int k = 0; k < L; k++) {
+                col[k * stride] = e;
+                e = ff_mul(e, t);
+            }
         }
-    }
 #pragma unroll 1
-    for (int k = L; k < KP; k++) col[k * T] = ff{0.0f, 0.0f};
+        for (int k = L; k < KP; k++) col[k * stride] = ff{0.0f, 0.0f};
+    }
 }
 
 // X: column x in registers of one thread (warp 0, x = lane), xv[k] for k < kNPow
@@ -579,7 +592,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
     SmemColl &sm = *reinterpret_cast<SmemColl *>(smraw);
     TileCommon &cm = sm.c;
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int m = tid, z = m / TY, y = m % TY;
+    const int m = tid;
     constexpr uint32_t kCols = 128;  // diagonals D2..D5: 32 columns each
     tc_setup(cm, kCols);
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
@@ -593,6 +606,8 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
         if (tile >= A.ntiles || cm.abort) break;
         const TileDesc td = A.tiles[tile];
         const LevelDev &lv = A.levels[td.level];
+        const TileShape sh(td.lz);
+        const int TY = sh.TY, TZ = sh.TZ, z = m >> sh.ly, y = m & (TY - 1);
         float acc_hi[TX], acc_lo[TX];
 #pragma unroll
         for (int x = 0; x < TX; x++) acc_hi[x] = acc_lo[x] = 0.0f;
@@ -642,7 +657,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                 {
                     const int npair = (L * (L + 1)) / 2;
                     for (int t = tid; t < TZ * npair; t += NTHR) {
-                        const int zz = t & (TZ - 1), q = t >> 4;
+                        const int zz = t & (TZ - 1), q = t >> sh.lz;
                         int b = 0, r = q;
                         while (r >= L - b) {
                             r -= L - b;
@@ -793,7 +808,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
     SmemInt &sm = *reinterpret_cast<SmemInt *>(smraw);
     TileCommon &cm = sm.c;
     const int tid = threadIdx.x, warp = tid >> 5;
-    const int m = tid, z = m / TY, y = m % TY;
+    const int m = tid;
     constexpr uint32_t kCols = 128;  // D2 (two K halves), D3, D4, D5: 16 columns each
     tc_setup(cm, kCols);
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
@@ -809,6 +824,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
         if (tile >= A.ntiles || cm.abort) break;
         const TileDesc td = A.tiles[tile];
         const LevelDev &lv = A.levels[td.level];
+        const TileShape sh(td.lz);
+        const int TY = sh.TY, TZ = sh.TZ, z = m >> sh.ly, y = m & (TY - 1);
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
         // this thread's V row, sliced once per tile (row exponent vm)
@@ -1018,7 +1035,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     while (q >= L - b) { q -= L - b; b++; }
                     const int a = q;
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
-#pragma unroll
+#pragma unroll 2
                     for (int yy = 0; yy < TY; yy += 2) {
                         s0 = ff_fma(sm.S[zz * TY + yy][a], cm.Y[b][yy], s0);
                         s1 = ff_fma(sm.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1], s1);
@@ -1046,7 +1063,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     }
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
                     const int pi = pair_index(L, b, a);
-#pragma unroll
+#pragma unroll 2
                     for (int zz = 0; zz < TZ; zz += 2) {
                         s0 = ff_fma(cm.Cxy[zz][pi], cm.Z[g][zz], s0);
                         s1 = ff_fma(cm.Cxy[zz + 1][pi], cm.Z[g][zz + 1], s1);
@@ -1093,8 +1110,9 @@ __global__ void k_item_images(const TileDesc *__restrict__ tiles, const int64_t 
             const TPair &p = *reinterpret_cast<const TPair *>(blob + (items[it] >> 16));
             int img[3][kMaxImages], n[3];
             axis_images(lv, 0, td.t[0], TX, p, img[0], n[0], status);
-            axis_images(lv, 1, td.t[1], TY, p, img[1], n[1], status);
-            axis_images(lv, 2, td.t[2], TZ, p, img[2], n[2], status);
+            const TileShape sh(td.lz);
+            axis_images(lv, 1, td.t[1], sh.TY, p, img[1], n[1], status);
+            axis_images(lv, 2, td.t[2], sh.TZ, p, img[2], n[2], status);
             ItemImg r;
             memset(&r, 0, sizeof r);
             r.nimg = n[0] | (n[1] << 8) | (n[2] << 16);
@@ -1160,12 +1178,13 @@ int mixed_build(TaskSet &ts, std::string &err) {
     for (int l = 0; l < P.nlevels; l++) {
         if (!P.lv[l].ortho) continue;
         ntx[l] = (P.lv[l].ngrid[0] + TX - 1) / TX;
-        nty[l] = (P.lv[l].ngrid[1] + TY - 1) / TY;
-        ntz[l] = (P.lv[l].ngrid[2] + TZ - 1) / TZ;
+        const TileShape sh(ts.tile_lz[l]);
+        nty[l] = (P.lv[l].ngrid[1] + sh.TY - 1) / sh.TY;
+        ntz[l] = (P.lv[l].ngrid[2] + sh.TZ - 1) / sh.TZ;
         lvl_first[l] = (int)tiles.size();
         for (int a = 0; a < ntz[l]; a++)
             for (int b = 0; b < nty[l]; b++)
-                for (int c = 0; c < ntx[l]; c++) tiles.push_back(TileDesc{l, {c, b, a}});
+                for (int c = 0; c < ntx[l]; c++) tiles.push_back(TileDesc{l, {c, b, a}, ts.tile_lz[l]});
     }
     const int ntiles = (int)tiles.size();
     std::vector<int64_t> count(ntiles + 1, 0);
@@ -1177,8 +1196,9 @@ int mixed_build(TaskSet &ts, std::string &err) {
             const PairGeom &g = ts.h_geom[k];
             const LevelDev &lv = P.lv[g.level];
             axis_tiles(lv, 0, g, TX, ax);
-            axis_tiles(lv, 1, g, TY, ay);
-            axis_tiles(lv, 2, g, TZ, az);
+            const TileShape sh(ts.tile_lz[g.level]);
+            axis_tiles(lv, 1, g, sh.TY, ay);
+            axis_tiles(lv, 2, g, sh.TZ, az);
             const int base = lvl_first[g.level];
             const double r2 = g.radius * g.radius * (1.0 + 1e-9) + 1e-12;
             const double hx = lv.dh[0][0], hy = lv.dh[1][1], hz = lv.dh[2][2];
@@ -1372,6 +1392,7 @@ static cudaError_t general_fp64(const TaskSet &ts, const GridPtrs &g, bool adj, 
 }
 
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
+    if (!ts.mixed) return cudaErrorNotSupported;
     const MixedState &M = *ts.mixed;
     cudaError_t e = cudaSuccess;
     if (M.northo > 0 && M.ntiles > 0) {
@@ -1387,6 +1408,7 @@ cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
 }
 
 cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
+    if (!ts.mixed) return cudaErrorNotSupported;
     const MixedState &M = *ts.mixed;
     cudaError_t e = cudaSuccess;
     if (M.northo > 0 && M.ntiles > 0) {

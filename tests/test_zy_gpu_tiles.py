@@ -1,0 +1,73 @@
+"""Tile shapes of the mixed path: every shape gives the FP64 results within the
+mixed-path bar, the shapes agree with each other, and the autotuner picks one
+of them and leaves the caller's buffers alone."""
+import numpy as np
+import pytest
+import torch
+
+from golden_io import rel_l2
+from gpu_util import run_collocate, run_integrate
+from libgpw_gb300 import autotune, capi, tasks as T
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-8
+
+
+@pytest.mark.parametrize("tz", [16, 8, 4])
+def test_shapes_match_fp64(tz):
+    wl = T.config(5, npairs=300, seed=21)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    g64 = run_collocate(wl, "fp64", ts=ts, plan=plan)[0]
+    V = wl.potentials(seed=4)
+    h64 = run_integrate(wl, V, "fp64", ts=ts, plan=plan)
+    ts.set_tiles([tz])
+    assert ts.tiles() == [tz]
+    gmx = run_collocate(wl, "mixed", ts=ts, plan=plan)[0]
+    assert rel_l2(gmx, g64) <= TOL
+    hmx = run_integrate(wl, V, "mixed", ts=ts, plan=plan)
+    assert np.abs(hmx - h64).max() <= TOL * np.abs(h64).max()
+
+
+def test_multigrid_per_level_shapes(oracle_lib):
+    wl = T.config(2, npairs=300)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    ts.set_tiles([4, 8, 16])
+    got = run_collocate(wl, "mixed", ts=ts, plan=plan)
+    want = oracle_lib.batch(wl, nthreads=8)
+    for g, w in zip(got, want):
+        assert rel_l2(g, w) <= TOL
+
+
+def test_bad_shape_rejected():
+    wl = T.config(1, npairs=20)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    with pytest.raises(capi.GpwError):
+        ts.set_tiles([32])
+    assert ts.tiles() == [8]  # the default shape
+
+
+def test_autotune_picks_a_candidate(tmp_path):
+    wl = T.config(5, npairs=2000, seed=5)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    dev = torch.device("cuda:0")
+    pab = torch.from_numpy(wl.pab).to(dev)
+    pab_before = pab.clone()
+    tz, ms = ts.autotune(pab)
+    assert tz[0] in (4, 8, 16) and ts.tiles() == tz
+    assert (ms[0] > 0).all()
+    assert torch.equal(pab, pab_before)
+    # the table path: first call tunes and records, the second reads it back
+    path = str(tmp_path / "tiles.json")
+    tz1, src1 = autotune.apply(ts, pab, path=path)
+    ts.set_tiles([16])
+    tz2, src2 = autotune.apply(ts, pab, path=path)
+    assert src1 == "tuned" and src2 == "table" and tz1 == tz2 == ts.tiles()
+    # results after tuning still match FP64
+    g64 = run_collocate(wl, "fp64", ts=ts, plan=plan)[0]
+    gmx = run_collocate(wl, "mixed", ts=ts, plan=plan)[0]
+    assert rel_l2(gmx, g64) <= TOL
