@@ -244,8 +244,8 @@ struct TileCommon {
     PairBuf pb[2];  // the current pair and the one being fetched
     ItemImg ii[2];  // their images over this tile
     ImgState im;    // images after the first of a multi-image item
-    ff Y[KP][kMaxTY];
-    ff Z[KP][kMaxTZ];
+    ff Y[KP][kMaxTY + 1];  // rows padded: lanes reading different rows hit different banks
+    ff Z[KP][kMaxTZ + 1];
     ff Cxy[kMaxTZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
     ff cxy_pad_[4];         // stage-2 reads up to 3 entries past a row
     int tile;
@@ -398,7 +398,7 @@ __device__ void build_yz(TileCommon &sm, const TPair &p, const ImgState &q, cons
     for (int ent = (int)threadIdx.x - 32; ent < sh.TY + sh.TZ; ent += 32) {
         const bool isy = ent < sh.TY;
         const int d = isy ? 1 : 2, i = isy ? ent : ent - sh.TY, T = isy ? sh.TY : sh.TZ;
-        const int stride = isy ? kMaxTY : kMaxTZ;
+        const int stride = isy ? kMaxTY + 1 : kMaxTZ + 1;
         ff *col = isy ? &sm.Y[0][i] : &sm.Z[0][i];
         const int g = q.o[d] + i;
         const bool in = i < min(T, lv.ngrid[d] - td.t[d] * T) && g >= p.lb[d] && g <= p.hi[d];
