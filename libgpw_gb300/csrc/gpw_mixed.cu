@@ -238,16 +238,20 @@ struct alignas(16) PairBuf {
     };
     float2 coef[2 * kCoef16Max];
 };
+// the record alone (integrate)
+struct alignas(16) PairHdr {
+    union {
+        TPair p;
+        uint4 hdr_[kHdr16];
+    };
+};
 
 // shared state of both tiled kernels
 struct TileCommon {
-    PairBuf pb[2];  // the current pair and the one being fetched
-    ItemImg ii[2];  // their images over this tile
+    ItemImg ii[2];  // images over this tile of the current pair and of the one being fetched
     ImgState im;    // images after the first of a multi-image item
-    ff Y[KP][kMaxTY + 1];  // rows padded: lanes reading different rows hit different banks
-    ff Z[KP][kMaxTZ + 1];
-    ff Cxy[kMaxTZ][NPAIR_MAX];  // collocate stage 1; integrate stage-2 output T[z][pair]
-    ff cxy_pad_[4];         // stage-2 reads up to 3 entries past a row
+    ff Y[kNPow][kMaxTY + 1];  // rows padded: lanes reading different rows hit different banks
+    ff Z[kNPow][kMaxTZ + 1];
     int tile;
     int img[3][kMaxImages];
     int nimg[3];
@@ -261,21 +265,33 @@ struct alignas(128) SmemColl {
     __half A[NSL][MROWS * KP];  // Cx slices, M=128 x K=16
     __half B[NSL][TX * KP];     // X slices, N=32 x K=16
     ff rc[NCOEF_MAX];           // coefficients re-expanded around the tile's column ic
+    ff Cxy[kMaxTZ][NPAIR_MAX];  // stage 1 output
+    ff cxy_pad_[4];             // stage-2 reads up to 3 entries past a row
+    PairBuf pb[2];              // the current pair and the one being fetched
     float bin[kNPow][kNPow];    // binomials C(a', a) of the re-expansion
     alignas(16) float cs[TX];   // 2^fx per column (0 for an empty column)
     TileCommon c;
 };
 
 struct alignas(128) SmemInt {
-    __half A[2][NSL][MROWS * KP];  // masked V slices, K halves x in [0,16) and [16,32)
-    __half B[2][NSL][KP * KP];     // X' slices, N=16 (alpha) x K=16 per half
-    __half Vs[2][NSL][MROWS * KP]; // this tile's V slices, unmasked, in the layout of A
-    ff S[MROWS][KP + 1];  // padded rows: conflict-free row-wise stores
+    union {
+        __half A[2][NSL][MROWS * KP];  // masked V slices, K halves x in [0,16) and [16,32)
+        struct {                       // after the MMAs have read A:
+            ff S[MROWS][KP + 1];       //   S[(z,y)][alpha], padded rows: conflict-free row stores
+            ff T[kMaxTZ][NPAIR_MAX];   //   stage-2 output T[z][(b,a)]
+        } st;
+    };
+    union {
+        __half B[2][NSL][KP * KP];        // X' slices, N=16 (alpha) x K=16 per half
+        float xmax[kNPow][TX + 4];        // |X[alpha][x]| for the per-alpha maxima, before B is written
+    };
+    __half Vs[2][NSL][MROWS * KP];  // this tile's V slices, unmasked, in the layout of A
     int gexp[KP];
-    alignas(16) float xmax[kNPow][TX + 4];  // |X[alpha][x]| for the per-alpha maxima (padded rows)
-    signed char rx0[MROWS], rx1[MROWS];     // each row's cube x range in the current image
+    signed char rx0[MROWS], rx1[MROWS];  // each row's cube x range in the current image
+    PairHdr pb[2];                       // the current pair's record and the one being fetched
     TileCommon c;
 };
+static_assert(sizeof(((SmemInt *)0)->st) <= sizeof(((SmemInt *)0)->A), "S and T fit in A");
 
 // pair index of (b, a), b + a <= lp, rows of constant b
 __device__ __forceinline__ int pair_index(int L, int b, int a) { return b * L - (b * (b - 1)) / 2 + a; }
@@ -297,12 +313,12 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // Starts copying item it into buf / ii: the pair's record, its coefficients when
 // with_coef, and the item's images.  Each thread waits for its own copies
 // (cp_async_wait_all) before the barrier after which the buffers are read.
-__device__ __forceinline__ void fetch_pair(PairBuf &buf, ItemImg &ii, const MixedArgs &A, int64_t it, uint64_t item,
+__device__ __forceinline__ void fetch_pair(uint4 *dst, ItemImg &ii, const MixedArgs &A, int64_t it, uint64_t item,
                                            bool with_coef) {
     const uint4 *src = A.blob + (item >> 16);
     const int n = with_coef ? min((int)(item & 0xFFFFu), kHdr16 + kCoef16Max) : kHdr16;
     const uint4 *isrc = reinterpret_cast<const uint4 *>(A.iimg + it);
-    uint4 *dst = buf.hdr_;  // the coefficients follow the record without a gap
+    // dst: the record's chunks, the coefficients following without a gap
     uint4 *idst = reinterpret_cast<uint4 *>(&ii);
     for (int t = threadIdx.x; t < n + 3; t += blockDim.x) {
         if (t < n) cp_async16(dst + t, src + t);
@@ -413,7 +429,7 @@ __device__ void build_yz(TileCommon &sm, const TPair &p, const ImgState &q, cons
             }
         }
 #pragma unroll 1
-        for (int k = L; k < KP; k++) col[k * stride] = ff{0.0f, 0.0f};
+        for (int k = L; k < kNPow; k++) col[k * stride] = ff{0.0f, 0.0f};
     }
 }
 
@@ -553,21 +569,23 @@ __device__ __forceinline__ bool tc_wait(TileCommon &c, uint32_t phase, int *stat
 
 // The pair loop of a tile: item it + 1 is copied while item it is processed.
 // Returns the buffer slot of item it once it is visible to all threads.
-__device__ __forceinline__ int next_pair(TileCommon &cm, const MixedArgs &A, int64_t it, int64_t it0, int64_t it1,
-                                         uint64_t &nxt, bool with_coef) {
+template <class Buf>
+__device__ __forceinline__ int next_pair(TileCommon &cm, Buf *pb, const MixedArgs &A, int64_t it, int64_t it0,
+                                         int64_t it1, uint64_t &nxt, bool with_coef) {
     const int cur = (int)((it - it0) & 1);
     cp_async_wait_all();
     __syncthreads();  // item it visible; every thread is done with the other slot
     if (it + 1 < it1) {
-        fetch_pair(cm.pb[cur ^ 1], cm.ii[cur ^ 1], A, it + 1, nxt, with_coef);
+        fetch_pair(pb[cur ^ 1].hdr_, cm.ii[cur ^ 1], A, it + 1, nxt, with_coef);
         if (it + 2 < it1) nxt = A.items[it + 2];
     }
     return cur;
 }
 
-__device__ __forceinline__ void first_pair(TileCommon &cm, const MixedArgs &A, int64_t it0, int64_t it1,
+template <class Buf>
+__device__ __forceinline__ void first_pair(TileCommon &cm, Buf *pb, const MixedArgs &A, int64_t it0, int64_t it1,
                                            uint64_t &nxt, bool with_coef) {
-    if (it0 < it1) fetch_pair(cm.pb[0], cm.ii[0], A, it0, A.items[it0], with_coef);
+    if (it0 < it1) fetch_pair(pb[0].hdr_, cm.ii[0], A, it0, A.items[it0], with_coef);
     if (it0 + 1 < it1) nxt = A.items[it0 + 1];
 }
 
@@ -615,10 +633,10 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
         const int64_t it0 = A.start[tile], it1 = A.start[tile + 1];
         uint64_t nxt = 0;
-        first_pair(cm, A, it0, it1, nxt, true);
+        first_pair(cm, sm.pb, A, it0, it1, nxt, true);
         for (int64_t it = it0; it < it1 && !cm.abort; it++) {
-            const int cur = next_pair(cm, A, it, it0, it1, nxt, true);
-            const PairBuf &pb = cm.pb[cur];
+            const int cur = next_pair(cm, sm.pb, A, it, it0, it1, nxt, true);
+            const PairBuf &pb = sm.pb[cur];
             const TPair &P = pb.p;
             const int L = P.L, lp = P.lp;
             const int nimg = item_images(cm, cm.ii[cur], P, lv, td, ext_x, A.status);
@@ -674,7 +692,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                             off = off1 + ((lp - g) * (lp - g + 1)) / 2 - b;
                         }
                         if (g <= n) s0 = ff_fma(sm.rc[off], cm.Z[g][zz], s0);
-                        cm.Cxy[zz][q] = ff_add(s0, s1);
+                        sm.Cxy[zz][q] = ff_add(s0, s1);
                     }
                 }
                 __syncthreads();
@@ -688,7 +706,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                 if (x0 <= x1) {
                     // b outer (runtime), a inner unrolled with a warp-uniform exit at lp - b:
                     // one compact loop body for every lp, up to kNPow independent updates
-                    const ff *crow = cm.Cxy[z];
+                    const ff *crow = sm.Cxy[z];
                     for (int b = 0; b <= lp; b++) {
                         const ff yb = cm.Y[b][y];
                         const ff *row = crow + pair_index(L, b, 0);
@@ -803,7 +821,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
     tc_teardown(cm, kCols, phase);
 }
 
-__global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
+__global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemInt &sm = *reinterpret_cast<SmemInt *>(smraw);
     TileCommon &cm = sm.c;
@@ -866,10 +884,10 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
         bool zero_row[2] = {false, false};  // A rows u, u + 64 hold zeros (warps 2-3)
         const int64_t it0 = A.start[tile], it1 = A.start[tile + 1];
         uint64_t nxt = 0;
-        first_pair(cm, A, it0, it1, nxt, false);
+        first_pair(cm, sm.pb, A, it0, it1, nxt, false);
         for (int64_t it = it0; it < it1 && !cm.abort; it++) {
-            const int cur = next_pair(cm, A, it, it0, it1, nxt, false);
-            const TPair &P = cm.pb[cur].p;
+            const int cur = next_pair(cm, sm.pb, A, it, it0, it1, nxt, false);
+            const TPair &P = sm.pb[cur].p;
             const int L = P.L, lp = P.lp;
             const int npair = (L * (L + 1)) / 2;
             const int64_t moff = P.coef_off;
@@ -1023,7 +1041,7 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                                 s = {__fmul_rn(t.hi, scl), __fmul_rn(t.lo, scl)};
                             }
                         }
-                        sm.S[m][a] = s;
+                        sm.st.S[m][a] = s;
                     }
                 }
                 tc::fence_before_sync();
@@ -1037,10 +1055,10 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
 #pragma unroll 2
                     for (int yy = 0; yy < TY; yy += 2) {
-                        s0 = ff_fma(sm.S[zz * TY + yy][a], cm.Y[b][yy], s0);
-                        s1 = ff_fma(sm.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1], s1);
+                        s0 = ff_fma(sm.st.S[zz * TY + yy][a], cm.Y[b][yy], s0);
+                        s1 = ff_fma(sm.st.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1], s1);
                     }
-                    cm.Cxy[zz][pair_index(L, b, a)] = ff_add(s0, s1);
+                    sm.st.T[zz][pair_index(L, b, a)] = ff_add(s0, s1);
                 }
                 __syncthreads();
                 // stage 1 transposed: W[g][b][a] += sum_z T[z][(b,a)] Z[g][z]
@@ -1065,8 +1083,8 @@ __global__ void __launch_bounds__(NTHR, 2) k_integrate_tiled(MixedArgs A) {
                     const int pi = pair_index(L, b, a);
 #pragma unroll 2
                     for (int zz = 0; zz < TZ; zz += 2) {
-                        s0 = ff_fma(cm.Cxy[zz][pi], cm.Z[g][zz], s0);
-                        s1 = ff_fma(cm.Cxy[zz + 1][pi], cm.Z[g][zz + 1], s1);
+                        s0 = ff_fma(sm.st.T[zz][pi], cm.Z[g][zz], s0);
+                        s1 = ff_fma(sm.st.T[zz + 1][pi], cm.Z[g][zz + 1], s1);
                     }
                     const ff s = ff_add(s0, s1);
                     if (s.hi != 0.0f) atomicAdd(A.mom + moff + t, (double)s.hi + (double)s.lo);
