@@ -134,11 +134,17 @@ __device__ __forceinline__ int fast_floor_checked(float rem, float r2f, float hi
     return (int)fl;
 }
 
+// the exact FP64 rule, out of line: taken only where the FP32 estimate is unsure
+__device__ __noinline__ int rule_jmax_exact(const TPair &p, int kf) { return rule_jmax(rule_remk(p.r2, kf, p.hz), p.hy); }
+__device__ __noinline__ int rule_imax_exact(const TPair &p, int kf, int jf) {
+    return rule_imax(rule_remk(p.r2, kf, p.hz), jf, p.hy, p.hx);
+}
+
 __device__ __forceinline__ int row_jmax(const TPair &p, int kf) {
     const float dz = (float)(-kf) * p.hzf;
     bool unsure;
     int j = fast_floor_checked(__fmaf_rn(-dz, dz, p.r2f), p.r2f, p.hyinvf, unsure);
-    if (unsure) j = rule_jmax(rule_remk(p.r2, kf, p.hz), p.hy);
+    if (unsure) j = rule_jmax_exact(p, kf);
     return j;
 }
 
@@ -146,7 +152,7 @@ __device__ __forceinline__ int row_imax(const TPair &p, int kf, int jf) {
     const float dz = (float)(-kf) * p.hzf, dy = (float)(-jf) * p.hyf;
     bool unsure;
     int i = fast_floor_checked(__fmaf_rn(-dy, dy, __fmaf_rn(-dz, dz, p.r2f)), p.r2f, p.hxinvf, unsure);
-    if (unsure) i = rule_imax(rule_remk(p.r2, kf, p.hz), jf, p.hy, p.hx);
+    if (unsure) i = rule_imax_exact(p, kf, jf);
     return i;
 }
 
@@ -590,15 +596,17 @@ __device__ __forceinline__ void first_pair(TileCommon &cm, Buf *pb, const MixedA
 }
 
 // images of the current item: 1 for the common case (state precomputed in ii);
-// for more, threads 0-2 derive them here (one extra barrier)
+// for more, threads 0-2 derive them here (one extra barrier, out of line)
+__device__ __noinline__ void item_images_multi(TileCommon &cm, const TPair &P, const LevelDev &lv,
+                                               const TileDesc &td, int ext_x, int *status) {
+    pair_images(cm, P, lv, td, ext_x, status);
+    __syncthreads();
+}
 __device__ __forceinline__ int item_images(TileCommon &cm, const ItemImg &ii, const TPair &P, const LevelDev &lv,
                                            const TileDesc &td, int ext_x, int *status) {
     const int np = ii.nimg;
     const int nimg = (np & 0xff) * ((np >> 8) & 0xff) * ((np >> 16) & 0xff);
-    if (nimg > 1) {
-        pair_images(cm, P, lv, td, ext_x, status);
-        __syncthreads();
-    }
+    if (nimg > 1) item_images_multi(cm, P, lv, td, ext_x, status);
     return nimg;
 }
 
