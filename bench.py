@@ -111,8 +111,8 @@ class Clocks:
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of this workload at
 # full size: profiles/dram_traffic_pairs1M_l4_256cubed.md
 TRAFFIC = {
-    ("pairs1M_l4_256cubed", 1000000, "k_integrate_tiled"): 11.860862e9 + 4.164775e9,
-    ("pairs1M_l4_256cubed", 1000000, "k_collocate_tiled"): 10.957352e9 + 0.160159e9,
+    ("pairs1M_l4_256cubed", 1000000, "k_collocate_tiled"): 12.741824e9 + 0.161365e9,
+    ("pairs1M_l4_256cubed", 1000000, "k_integrate_tiled"): 11.204862e9 + 3.773629e9,
 }
 
 
