@@ -396,7 +396,7 @@ def main():
                 "frac": achieved_tf / peak, "traffic": TRAFFIC.get((wl.name, wl.ntasks, kname)),
                 "peak_source": "bf16 sustained, MEASURED_PEAKS.json (of measured)",
                 "limiter": "FP32/integer instruction issue of the float-float stages, not the tensor pipe "
-                           "(tensor pipe active ~3%, issue active 44% collocate / 28% integrate in the ncu captures)"}
+                           "(tensor pipe active ~4%, issue slots busy 47% collocate / 39% integrate in the ncu captures)"}
     else:
         hbm = peaks.get("hbm_gbs") or 6800.0
         gbytes_alg = 16.0 * points  # FP64 read+write per cube point (no reuse)
