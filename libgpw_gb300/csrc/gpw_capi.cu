@@ -478,6 +478,17 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
         T->chunks.push_back(c);
         k = m;
     }
+    // general-cell pairs (sorted after the orthorhombic ones) for the float-float kernel
+    for (int64_t m = 0; m < ntasks; m++) {
+        if (T->h_geom[m].ortho) continue;
+        if (T->gen_count == 0) T->gen_first = (int)m;
+        T->gen_count++;
+        T->gen_smem = std::max(T->gen_smem, smem_general_ff(T->h_geom[m]));
+    }
+    if (T->gen_smem > smem_limit) {
+        delete T;
+        return fail(GPW_ERR_UNSUPPORTED, "gpw_taskset_create: a general-cell cube is too large for one CTA");
+    }
     if (smem_prep(T->max_A, T->max_B) > smem_limit) {
         delete T;
         return fail(GPW_ERR_UNSUPPORTED, "gpw_taskset_create: angular momenta too high for the set-up kernel");

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "gpw_coef.cuh"
+#include "gpw_ff.cuh"
 #include "gpw_internal.h"
 
 namespace gpw {
@@ -467,6 +468,172 @@ k_general_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// General cell in float-float (the mixed path): the structure of k_general_fp64
+// -- one CTA per pair, the lattice-basis polynomial contracted over k, then j,
+// per row of the index box, the row's i-range from the reference's quadratic
+// (FP64, general_row, so the point set is the reference's) -- with every
+// per-point operation in float-float instead of FP64 (GB300 runs FP64 at ~1/64
+// of its FP32 rate):
+//   r^2(di) = G00 di^2 + A1 di + A0 per row (metric G = dh dh^T; A1, A0 per row
+//   in FP64, split to float-float), exp(-zetp r^2) by ff_exp, the polynomial in
+//   di by Horner; collocate adds hi + lo to the grid with FP64 atomics,
+//   integrate reduces V exp(..) di^n over each row with warp shuffles.
+__device__ __forceinline__ ff ff_shfl_xor(ff v, int o) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+template <bool kAdj>
+__global__ void __launch_bounds__(256)
+k_general_ff(const PairGeom *__restrict__ geoms, int first, const LevelDev *__restrict__ levels,
+             const double *__restrict__ coef, double *__restrict__ mom, GridPtrs grids, int *status) {
+    extern __shared__ double smd[];
+    const PairGeom g = geoms[first + blockIdx.x];
+    const LevelDev &lv = levels[g.level];
+    double *__restrict__ grid = grids.p[g.level];
+    const int lp = g.lp, L = lp + 1;
+    const int ny = g.hi[1] - g.cc[1] + 1;
+    ff *Q = reinterpret_cast<ff *>(smd);  // [k][j][i] dense
+    ff *Qjk = Q + L * L * L;              // [j][i]
+    ff *Qj = Qjk + L * L;                 // [row][i]
+    ff *rc = Qj + ny * L;                 // per row: a1, a0, d0 (r^2 along the row, first di)
+    int *rows = reinterpret_cast<int *>(rc + 3 * ny);  // ismin, ismax, jidx
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+    for (int t = tid; t < L * L * L; t += nthr) {
+        const int i = t % L, j = (t / L) % L, k = t / (L * L);
+        Q[t] = (!kAdj && i + j + k <= lp) ? ff_from_double(coef[g.coef_off + pidx(lp, k, j, i)]) : ff{0.0f, 0.0f};
+    }
+    // metric of the lattice steps
+    double G[3][3];
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 3; b++) G[a][b] = lv.dh[a][0] * lv.dh[b][0] + lv.dh[a][1] * lv.dh[b][1] + lv.dh[a][2] * lv.dh[b][2];
+    const ff g00 = ff_from_double(G[0][0]);
+    const ff mz = ff_from_double(-g.zetp);
+    __syncthreads();
+    int off[3];
+    for (int d = 0; d < 3; d++) off[d] = imod(g.cc[d] + lv.lb_grid[d], lv.npts[d]);
+    for (int kk = g.cc[2]; kk <= g.hi[2]; kk++) {
+        const double dk = rsub((double)kk, g.off[2]);
+        const int kidx = lv.periodic[2] ? imod(kk, lv.npts[2]) : kk - g.cc[2] + off[2];
+        if (kidx < 0 || kidx >= lv.ngrid[2]) {
+            if (tid == 0) atomicOr(status, kStatOutOfWindow);
+            continue;
+        }
+        const ff dkf = ff_from_double(dk);
+        if (!kAdj) {
+            for (int t = tid; t < L * L; t += nthr) {
+                const int i = t % L, j = t / L;
+                ff s = {0.0f, 0.0f};
+                for (int k = lp - i - j; k >= 0; k--) s = ff_fma(s, dkf, Q[(k * L + j) * L + i]);
+                Qjk[t] = s;
+            }
+            __syncthreads();
+        }
+        // rows: the reference's i-range (FP64 quadratic), one row per lane
+        for (int row = tid; row < ny; row += nthr) {
+            const int jj = g.cc[1] + row;
+            const double dj = rsub((double)jj, g.off[1]);
+            int ismin = 0, ismax = -1;
+            if (!general_row(lv.dh, g.off, dj, dk, g.radius, ismin, ismax)) { ismin = 0; ismax = -1; }
+            rows[3 * row] = ismin;
+            rows[3 * row + 1] = ismax;
+            rows[3 * row + 2] = lv.periodic[1] ? imod(jj, lv.npts[1]) : jj - g.cc[1] + off[1];
+            // r^2 = G00 di^2 + A1 di + A0 along the row; di = (ismin - off0) + n
+            rc[3 * row] = ff_from_double(2.0 * (G[0][1] * dj + G[0][2] * dk));
+            rc[3 * row + 1] = ff_from_double(G[1][1] * dj * dj + 2.0 * G[1][2] * dj * dk + G[2][2] * dk * dk);
+            rc[3 * row + 2] = ff_from_double((double)ismin - g.off[0]);
+        }
+        if (!kAdj) {
+            for (int t = tid; t < ny * L; t += nthr) {
+                const int row = t / L, i = t % L;
+                const ff djf = ff_from_double(rsub((double)(g.cc[1] + row), g.off[1]));
+                ff s = {0.0f, 0.0f};
+                for (int j = lp - i; j >= 0; j--) s = ff_fma(s, djf, Qjk[j * L + i]);
+                Qj[t] = s;
+            }
+        }
+        __syncthreads();
+        for (int row = warp; row < ny; row += nwarp) {
+            const int ismin = rows[3 * row], ismax = rows[3 * row + 1], jidx = rows[3 * row + 2];
+            if (ismax < ismin) continue;
+            if (jidx < 0 || jidx >= lv.ngrid[1]) {
+                if (lane == 0) atomicOr(status, kStatOutOfWindow);
+                continue;
+            }
+            const ff a1 = rc[3 * row], a0 = rc[3 * row + 1], d0 = rc[3 * row + 2];
+            const int64_t rowbase = ((int64_t)kidx * lv.ngrid[1] + jidx) * lv.ngrid[0];
+            ff acc[kNPow];
+#pragma unroll
+            for (int n = 0; n < kNPow; n++) acc[n] = ff{0.0f, 0.0f};
+            for (int ii = ismin + lane; ii <= ismax; ii += 32) {
+                const int iidx = lv.periodic[0] ? imod(ii, lv.npts[0]) : ii - g.cc[0] + off[0];
+                if (iidx < 0 || iidx >= lv.ngrid[0]) {
+                    atomicOr(status, kStatOutOfWindow);
+                    continue;
+                }
+                const ff di = ff_add(d0, ff{(float)(ii - ismin), 0.0f});
+                const ff r2 = ff_fma(ff_fma(g00, di, a1), di, a0);
+                const ff e = ff_exp(ff_mul(r2, mz));
+                if (!kAdj) {
+                    ff s = Qj[row * L + lp];
+                    for (int n = lp - 1; n >= 0; n--) s = ff_fma(s, di, Qj[row * L + n]);
+                    const ff v = ff_mul(s, e);
+                    atomicAdd(grid + rowbase + iidx, (double)v.hi + (double)v.lo);
+                } else {
+                    ff p = ff_mul(ff_from_double(grid[rowbase + iidx]), e);
+#pragma unroll
+                    for (int n = 0; n < kNPow; n++) {  // L is uniform over the CTA
+                        if (n >= L) break;
+                        acc[n] = ff_add(acc[n], p);
+                        p = ff_mul(p, di);
+                    }
+                }
+            }
+            if (kAdj) {
+#pragma unroll
+                for (int n = 0; n < kNPow; n++) {
+                    if (n >= L) break;
+                    ff v = acc[n];
+                    for (int o = 16; o > 0; o >>= 1) v = ff_add(v, ff_shfl_xor(v, o));
+                    acc[n] = v;
+                }
+                if (lane == 0)
+                    for (int n = 0; n < L; n++) Qj[row * L + n] = acc[n];
+            }
+        }
+        __syncthreads();
+        if (kAdj) {
+            // Qjk[j][i] = sum_rows Qj[row][i] dj^j;  Q[k][j][i] += Qjk[j][i] dk^k
+            for (int t = tid; t < L * L; t += nthr) {
+                const int i = t % L, j = t / L;
+                if (i + j > lp) continue;
+                ff s = {0.0f, 0.0f};
+                for (int row = 0; row < ny; row++) {
+                    if (rows[3 * row + 1] < rows[3 * row]) continue;
+                    const ff djf = ff_from_double((double)(g.cc[1] + row) - g.off[1]);
+                    ff p = {1.0f, 0.0f};
+                    for (int e = 0; e < j; e++) p = ff_mul(p, djf);
+                    s = ff_fma(Qj[row * L + i], p, s);
+                }
+                ff p = {1.0f, 0.0f};
+                for (int k = 0; k <= lp - i - j; k++) {
+                    Q[(k * L + j) * L + i] = ff_fma(s, p, Q[(k * L + j) * L + i]);
+                    p = ff_mul(p, dkf);
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (kAdj) {
+        for (int t = tid; t < L * L * L; t += nthr) {
+            const int i = t % L, j = (t / L) % L, k = t / (L * L);
+            if (i + j + k <= lp) mom[g.coef_off + pidx(lp, k, j, i)] = (double)Q[t].hi + (double)Q[t].lo;
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 static cudaError_t set_smem(const void *fn, int bytes) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -477,7 +644,8 @@ static cudaError_t set_smem(const void *fn, int bytes) {
 cudaError_t fp64_kernel_attributes(int smem_max) {
     const void *fns[] = {(const void *)k_prep, (const void *)k_backtransform,
                          (const void *)k_ortho_fp64<false>, (const void *)k_ortho_fp64<true>,
-                         (const void *)k_general_fp64<false>, (const void *)k_general_fp64<true>};
+                         (const void *)k_general_fp64<false>, (const void *)k_general_fp64<true>,
+                         (const void *)k_general_ff<false>, (const void *)k_general_ff<true>};
     for (const void *fn : fns) {
         cudaError_t e = set_smem(fn, smem_max);
         if (e != cudaSuccess) return e;
@@ -529,6 +697,26 @@ static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool a
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+
+// general-cell pairs of a mixed call: the float-float kernel
+int smem_general_ff(const PairGeom &g) {
+    const int L = g.lp + 1;
+    const int ny = g.hi[1] - g.cc[1] + 1;
+    return 8 * (L * L * L + L * L + ny * L + 3 * ny) + 12 * ny;
+}
+
+// one launch over all general-cell pairs (contiguous in the sorted order)
+cudaError_t launch_general_ff(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s) {
+    if (ts.gen_count == 0) return cudaSuccess;
+    ProfScope prof(ts, s);
+    if (adj)
+        k_general_ff<true><<<ts.gen_count, 256, ts.gen_smem, s>>>(ts.d_geom, ts.gen_first, ts.plan->d_levels,
+                                                                 ts.d_coef, ts.d_mom, g, ts.d_status);
+    else
+        k_general_ff<false><<<ts.gen_count, 256, ts.gen_smem, s>>>(ts.d_geom, ts.gen_first, ts.plan->d_levels,
+                                                                  ts.d_coef, ts.d_mom, g, ts.d_status);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_fp64_kind(const TaskSet &ts, const GridPtrs &g, bool adj, int kind, cudaStream_t s) {

@@ -53,6 +53,7 @@ struct TaskSet {
     std::vector<Chunk> chunks;     // FP64 launches
     MixedState *mixed = nullptr;
     int tile_lz[GPW_MAX_LEVELS];   // tiled path: log2 of the tile's z extent per level
+    int gen_first = 0, gen_count = 0, gen_smem = 0;  // general-cell pairs (float-float kernel)
     // profiling (gpw_taskset_profile / gpw_taskset_stats)
     bool profile = false;
     mutable std::vector<cudaEvent_t> ev_pool;
@@ -108,6 +109,8 @@ cudaError_t launch_integrate_core(const int length[3], int L, const double *pol,
 int mixed_build(TaskSet &ts, std::string &err);
 void mixed_free(TaskSet &ts);
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
+cudaError_t launch_general_ff(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s);
+int smem_general_ff(const PairGeom &g);
 cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 
 // gpw_capi.cu (host helpers)

@@ -1412,9 +1412,9 @@ static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which) {
     return a;
 }
 
-// general-cell pairs of a mixed call run on the FP64 kernels
-static cudaError_t general_fp64(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s) {
-    return adj ? launch_fp64_kind(ts, g, true, 1, s) : launch_fp64_kind(ts, g, false, 1, s);
+// general-cell pairs of a mixed call run on the float-float general kernel
+static cudaError_t general_ff(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s) {
+    return launch_general_ff(ts, g, adj, s);
 }
 
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
@@ -1430,7 +1430,7 @@ cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
         k_collocate_tiled<<<M.grid_ctas, NTHR, sizeof(SmemColl), s>>>(make_args(ts, g, 0));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    return general_fp64(ts, g, false, s);
+    return general_ff(ts, g, false, s);
 }
 
 cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
@@ -1444,7 +1444,7 @@ cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
         k_integrate_tiled<<<M.grid_ctas_i, NTHR, sizeof(SmemInt), s>>>(make_args(ts, g, 1));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-    return general_fp64(ts, g, true, s);
+    return general_ff(ts, g, true, s);
 }
 
 }  // namespace gpw
