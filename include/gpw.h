@@ -178,7 +178,7 @@ int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
 
 /*
  * Tile shapes of the mixed-precision (tiled) path.  Each orthorhombic level is
- * cut into tiles of 32 x (128 / tz) x tz grid points (x, y, z), tz = 4, 8 or 16;
+ * cut into tiles of 32 x (128 / tz) x tz grid points (x, y, z), tz = 4 or 8;
  * the shape sets how many tiles a cube touches and how much per-tile work a pair
  * costs.  No reference counterpart: the reference has no tiled path; the shapes
  * change the speed, not the results beyond rounding.
@@ -191,7 +191,7 @@ int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
  * `stream` for each candidate tz of each level that holds orthorhombic tasks
  * (one level at a time, the others at their best so far), keeps the fastest
  * and writes tz per level to tile_z (may be NULL) and the measured ms to
- * ms[3 * level + c] for the candidates tz = 16, 8, 4 (-1 where not timed; may
+ * ms[2 * level + c] for the candidates tz = 8, 4 (-1 where not timed; may
  * be NULL).  d_pab is a density buffer as for gpw_collocate.  The timed calls
  * run on scratch grids and matrix elements allocated here; the caller's
  * buffers are not written.

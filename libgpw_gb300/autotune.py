@@ -1,7 +1,7 @@
 """Tile-shape autotuner of the mixed-precision path, with a JSON table.
 
 The tiled kernels cut every orthorhombic grid level into tiles of 32 x (128/tz)
-x tz points; tz (4, 8 or 16) trades the number of tiles a cube touches against
+x tz points; tz (4 or 8) trades the number of tiles a cube touches against
 the per-tile work of a pair.  ``gpw_taskset_autotune`` times one collocate +
 integrate per candidate and level on the device.  This module keys the result
 by a workload signature (grid levels and the task set's size, angular momentum
@@ -72,7 +72,7 @@ def apply(ts, pab, tasks=None, path: str | None = None, tune: bool = True) -> tu
     if not tune:
         return ts.tiles(), "default"
     tz, ms = ts.autotune(pab)
-    table[key] = {"tile_z": tz, "ms": [[round(float(v), 3) for v in row] for row in ms], "candidates_tz": [16, 8, 4]}
+    table[key] = {"tile_z": tz, "ms": [[round(float(v), 3) for v in row] for row in ms], "candidates_tz": [8, 4]}
     try:
         save_table(table, path)
     except OSError:

@@ -610,12 +610,13 @@ int gpw_taskset_check(gpw_taskset *ts, void *stream) {
     if (h & kStatOutOfWindow) return fail(GPW_ERR_OUT_OF_WINDOW, "a cube left the local grid window");
     if (h & kStatTimeout) return fail(GPW_ERR_TIMEOUT, "a bounded device wait gave up");
     if (h & kStatBadTable) return fail(GPW_ERR_INVALID_ARG, "a cube list was inconsistent on the device");
+    if (h & kStatBadTile) return fail(GPW_ERR_INVALID_ARG, "a tile shape the collocate kernel does not hold");
     if (h & kStatTooManyImages)
         return fail(GPW_ERR_UNSUPPORTED, "a cube spans more periodic images than the tiled path handles");
     return GPW_SUCCESS;
 }
 
-static int tile_lz_of(int tz) { return tz == 4 ? 2 : tz == 8 ? 3 : tz == 16 ? 4 : -1; }
+static int tile_lz_of(int tz) { return tz == 4 ? 2 : tz == 8 ? 3 : -1; }
 
 static int retile(gpw_taskset *ts, const int *lz) {
     bool same = true;
@@ -636,7 +637,7 @@ int gpw_taskset_set_tiles(gpw_taskset *ts, const int *tile_z) {
     int lz[GPW_MAX_LEVELS];
     for (int l = 0; l < ts->plan->nlevels; l++) {
         lz[l] = tile_lz_of(tile_z[l]);
-        if (lz[l] < 0) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_set_tiles: tile z extent must be 4, 8 or 16");
+        if (lz[l] < 0) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_set_tiles: tile z extent must be 4 or 8");
     }
     return retile(ts, lz);
 }
@@ -664,7 +665,7 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
     if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
     if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
     int st = ce == cudaSuccess ? GPW_SUCCESS : cuda_fail(ce, "gpw_taskset_autotune");
-    static const int cand[3] = {4, 3, 2};  // TZ = 16, 8, 4
+    static const int cand[2] = {3, 2};  // TZ = 8, 4
     int best[GPW_MAX_LEVELS];
     for (int l = 0; l < P.nlevels; l++) best[l] = ts->tile_lz[l];
     auto time_once = [&](float &out) -> int {
@@ -684,7 +685,7 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
         bool used = false;  // levels without orthorhombic tasks keep their shape
         for (int64_t k = 0; k < ts->ntasks && !used; k++) used = ts->h_geom[k].ortho && ts->h_geom[k].level == l;
         float best_ms = -1.0f;
-        for (int c = 0; c < 3 && !st; c++) {
+        for (int c = 0; c < 2 && !st; c++) {
             float t = 0.0f;
             if (used) {
                 int lz[GPW_MAX_LEVELS];
@@ -694,7 +695,7 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
                 if (!st) st = time_once(t);
                 if (!st && (best_ms < 0.0f || t < best_ms)) best_ms = t, best[l] = cand[c];
             }
-            if (ms) ms[3 * l + c] = used ? (double)t : -1.0;
+            if (ms) ms[2 * l + c] = used ? (double)t : -1.0;
         }
     }
     if (!st) st = retile(ts, best);

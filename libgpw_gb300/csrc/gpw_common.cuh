@@ -164,6 +164,7 @@ enum : int {
     kStatTimeout = 2,
     kStatBadTable = 4,
     kStatTooManyImages = 8,
+    kStatBadTile = 16,
 };
 
 }  // namespace gpw

@@ -1,7 +1,7 @@
 // Tiled mixed-precision collocate / integrate.
 //
 // Each CTA owns one tile of one grid level (TX x TY x TZ points, x fastest; TX = 32,
-// TY x TZ = 128 rows with TZ = 4, 8 or 16 per level, chosen by the tile autotuner) and
+// TY x TZ = 128 rows with TZ = 4 or 8 per level, chosen by the tile autotuner) and
 // walks every pair whose cube touches the tile.  Per pair and tile:
 //   1-D tables t^k exp(-zetp t^2) over the tile's three ranges   (float-float)
 //   stage 1  Cxy[z][b][a] = sum_g c[g][b][a] Z[g][z]              (float-float)
@@ -41,6 +41,7 @@ namespace gpw {
 constexpr int TX = 32;
 constexpr int MROWS = 128;       // TY * TZ rows per tile, one per thread
 constexpr int kMaxTY = 32, kMaxTZ = 16;
+constexpr int kMaxTZColl = 8;  // collocate keeps its stage-1 output for at most 8 z (tiles with TZ <= 8)
 constexpr int NTHR = MROWS;
 constexpr int NSL = 4;          // slices per operand
 constexpr int SLB = 10;         // bits per slice
@@ -271,9 +272,10 @@ struct alignas(128) SmemColl {
     __half A[NSL][MROWS * KP];  // Cx slices, M=128 x K=16
     __half B[NSL][TX * KP];     // X slices, N=32 x K=16
     ff rc[NCOEF_MAX];           // coefficients re-expanded around the tile's column ic
-    ff Cxy[kMaxTZ][NPAIR_MAX];  // stage 1 output
+    ff Cxy[kMaxTZColl][NPAIR_MAX];  // stage 1 output
     ff cxy_pad_[4];             // stage-2 reads up to 3 entries past a row
     PairBuf pb[2];              // the current pair and the one being fetched
+    float acc_lo[MROWS][TX + 1];  // low parts of the tile sums (row m belongs to thread m; padded rows)
     float bin[kNPow][kNPow];    // binomials C(a', a) of the re-expansion
     alignas(16) float cs[TX];   // 2^fx per column (0 for an empty column)
     TileCommon c;
@@ -613,7 +615,7 @@ __device__ __forceinline__ int item_images(TileCommon &cm, const ItemImg &ii, co
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
+__global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemColl &sm = *reinterpret_cast<SmemColl *>(smraw);
     TileCommon &cm = sm.c;
@@ -634,7 +636,12 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
         const LevelDev &lv = A.levels[td.level];
         const TileShape sh(td.lz);
         const int TY = sh.TY, TZ = sh.TZ, z = m >> sh.ly, y = m & (TY - 1);
-        float acc_hi[TX], acc_lo[TX];
+        if (TZ > kMaxTZColl) {  // shapes are validated on the host; never taken
+            if (tid == 0) atomicOr(A.status, kStatBadTile);
+            continue;
+        }
+        float acc_hi[TX];  // the low parts live in shared memory (registers for 4 CTAs per SM)
+        float *acc_lo = sm.acc_lo[m];
 #pragma unroll
         for (int x = 0; x < TX; x++) acc_hi[x] = acc_lo[x] = 0.0f;
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
@@ -804,7 +811,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_collocate_tiled(MixedArgs A) {
                             const float sv = __fadd_rn(acc_hi[x], hi);
                             const float bb = __fsub_rn(sv, acc_hi[x]);
                             const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
-                            acc_lo[x] = in ? __fadd_rn(acc_lo[x], __fadd_rn(err, lo)) : acc_lo[x];
+                            if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
                             acc_hi[x] = in ? sv : acc_hi[x];
                         }
                     }
