@@ -104,3 +104,67 @@ def test_mixed_general_sets_vs_fp64(name):
     h64 = run_integrate(wl, V, "fp64", ts=ts, plan=plan)
     hmx = run_integrate(wl, V, "mixed", ts=ts, plan=plan)
     assert np.abs(hmx - h64).max() <= TOL * np.abs(h64).max()
+
+def test_mixed_empty_and_repeat():
+    """No pairs: the grid stays zero; a second call accumulates (grid += rho)."""
+    wl = T.config(1, npairs=1)
+    wl.tasks = wl.tasks[:0]
+    assert not np.any(run_collocate(wl, "mixed")[0])
+    import torch
+
+    wl = T.config(4, npairs=60)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    dev = torch.device("cuda:0")
+    pab = torch.from_numpy(wl.pab).to(dev)
+    g = torch.zeros(T.grid_shape(wl.levels[0]), dtype=torch.float64, device=dev)
+    ts.collocate(pab, [g], "mixed")
+    once = g.clone()
+    ts.collocate(pab, [g], "mixed")
+    ts.check()
+    assert rel_l2(g.cpu().numpy(), 2 * once.cpu().numpy()) <= 1e-15
+
+
+def test_mixed_cubes_larger_than_the_cell(oracle_lib):
+    """Broad Gaussians on a small periodic cell: a cube wraps several times, so a
+    tile sees several images of one pair (the multi-image path)."""
+    wl = T.synthetic("wrap", 40, 2, (0.2, 0.6), 6.0, [(32, 32, 32)], seed=11)
+    got = run_collocate(wl, "mixed")[0]
+    want = oracle_lib.batch(wl, nthreads=8)[0]
+    assert rel_l2(got, want) <= TOL
+    V = wl.potentials(seed=8)
+    h = run_integrate(wl, V, "mixed")
+    hw = oracle_lib.batch(wl, V=V, nthreads=8)
+    assert np.abs(h - hw).max() <= TOL * np.abs(hw).max()
+
+
+def test_mixed_linearity_and_adjointness_at_scale():
+    """Size-independent properties on 20k pairs of the 1M-pair distributions
+    (256^3): collocate is linear in the density blocks, and
+    <V, collocate(P)> = <integrate(V), P>."""
+    import torch
+
+    wl = T.config(5, npairs=20000, seed=99)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    dev = torch.device("cuda:0")
+    pab = torch.from_numpy(wl.pab).to(dev)
+    shape = T.grid_shape(wl.levels[0])
+    g1 = torch.zeros(shape, dtype=torch.float64, device=dev)
+    g2 = torch.zeros(shape, dtype=torch.float64, device=dev)
+    ts.collocate(pab, [g1], "mixed")
+    ts.collocate(-2.0 * pab, [g2], "mixed")  # a power of two scales every slice exactly
+    ts.check()
+    n1 = torch.linalg.vector_norm(g1)
+    assert float(torch.linalg.vector_norm(g2 + 2.0 * g1) / n1) <= 1e-15
+    g2.zero_()
+    ts.collocate(-3.0 * pab, [g2], "mixed")  # otherwise within the path's precision
+    ts.check()
+    assert float(torch.linalg.vector_norm(g2 + 3.0 * g1) / n1) <= TOL
+    V = torch.from_numpy(wl.potentials(seed=12)[0]).to(dev)
+    hab = torch.zeros(ts.pab_extent, dtype=torch.float64, device=dev)
+    ts.integrate([V], hab, "mixed")
+    ts.check()
+    lhs = float(torch.sum(V * g1))
+    rhs = float(torch.sum(hab * pab[: ts.pab_extent]))
+    assert abs(lhs - rhs) <= TOL * max(abs(lhs), float(torch.sum(torch.abs(V * g1))) * 1e-3)
