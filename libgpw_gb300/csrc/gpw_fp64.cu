@@ -498,7 +498,8 @@ k_general_ff(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
     ff *Qjk = Q + L * L * L;              // [j][i]
     ff *Qj = Qjk + L * L;                 // [row][i]
     ff *rc = Qj + ny * L;                 // per row: a1, a0, d0 (r^2 along the row, first di)
-    int *rows = reinterpret_cast<int *>(rc + 3 * ny);  // ismin, ismax, jidx
+    ff *powj = rc + 3 * ny;               // integrate: per row dj^j, j <= lp
+    int *rows = reinterpret_cast<int *>(powj + ny * L);  // ismin, ismax, jidx
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
     for (int t = tid; t < L * L * L; t += nthr) {
@@ -544,6 +545,14 @@ k_general_ff(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
             rc[3 * row] = ff_from_double(2.0 * (G[0][1] * dj + G[0][2] * dk));
             rc[3 * row + 1] = ff_from_double(G[1][1] * dj * dj + 2.0 * G[1][2] * dj * dk + G[2][2] * dk * dk);
             rc[3 * row + 2] = ff_from_double((double)ismin - g.off[0]);
+            if (kAdj) {
+                const ff djf = ff_from_double(dj);
+                ff p = {1.0f, 0.0f};
+                for (int j = 0; j <= lp; j++) {
+                    powj[row * L + j] = p;
+                    p = ff_mul(p, djf);
+                }
+            }
         }
         if (!kAdj) {
             for (int t = tid; t < ny * L; t += nthr) {
@@ -612,10 +621,7 @@ k_general_ff(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
                 ff s = {0.0f, 0.0f};
                 for (int row = 0; row < ny; row++) {
                     if (rows[3 * row + 1] < rows[3 * row]) continue;
-                    const ff djf = ff_from_double((double)(g.cc[1] + row) - g.off[1]);
-                    ff p = {1.0f, 0.0f};
-                    for (int e = 0; e < j; e++) p = ff_mul(p, djf);
-                    s = ff_fma(Qj[row * L + i], p, s);
+                    s = ff_fma(Qj[row * L + i], powj[row * L + j], s);
                 }
                 ff p = {1.0f, 0.0f};
                 for (int k = 0; k <= lp - i - j; k++) {
@@ -703,7 +709,7 @@ static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool a
 int smem_general_ff(const PairGeom &g) {
     const int L = g.lp + 1;
     const int ny = g.hi[1] - g.cc[1] + 1;
-    return 8 * (L * L * L + L * L + ny * L + 3 * ny) + 12 * ny;
+    return 8 * (L * L * L + L * L + 2 * ny * L + 3 * ny) + 12 * ny;
 }
 
 // one launch over all general-cell pairs (contiguous in the sorted order)
