@@ -177,24 +177,26 @@ int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
                       int64_t *contraction_launches, int64_t *kernel_launches);
 
 /*
- * Tile shapes of the mixed-precision (tiled) path.  Each orthorhombic level is
- * cut into tiles of 32 x (128 / tz) x tz grid points (x, y, z), tz = 4 or 8;
- * the shape sets how many tiles a cube touches and how much per-tile work a pair
- * costs.  No reference counterpart: the reference has no tiled path; the shapes
- * change the speed, not the results beyond rounding.
+ * Tile shapes of the mixed-precision (tiled) path.  A level is cut into tiles
+ * of 32 x (128 / tz) x tz grid points (x, y, z), tz = 4 or 8; the shape sets
+ * how many tiles a cube touches and how much per-tile work a pair costs.  A
+ * general-cell level may also take tz = 0 (its default): no tiles, its pairs
+ * run on the float-float kernel, one CTA per pair.  No reference counterpart:
+ * the reference has no tiled path; the shapes change the speed, not the
+ * results beyond rounding.
  *
  * gpw_taskset_set_tiles takes tz per level (nlevels entries) and re-bins the
  * task set; gpw_taskset_get_tiles returns the current tz per level.  Both wait
  * for the device: call them when no launch of this task set is in flight.
  *
  * gpw_taskset_autotune times one mixed collocate + integrate of the task set on
- * `stream` for each candidate tz of each level that holds orthorhombic tasks
- * (one level at a time, the others at their best so far), keeps the fastest
- * and writes tz per level to tile_z (may be NULL) and the measured ms to
- * ms[2 * level + c] for the candidates tz = 8, 4 (-1 where not timed; may
- * be NULL).  d_pab is a density buffer as for gpw_collocate.  The timed calls
- * run on scratch grids and matrix elements allocated here; the caller's
- * buffers are not written.
+ * `stream` for each candidate tz of each level that holds tasks (one level at
+ * a time, the others at their best so far), keeps the fastest and writes tz
+ * per level to tile_z (may be NULL) and the measured ms to ms[3 * level + c]
+ * for the candidates tz = 8, 4, 0 (tz = 0 on general-cell levels only; -1
+ * where not timed; may be NULL).  d_pab is a density buffer as for
+ * gpw_collocate.  The timed calls run on scratch grids and matrix elements
+ * allocated here; the caller's buffers are not written.
  */
 int gpw_taskset_set_tiles(gpw_taskset *ts, const int *tile_z);
 int gpw_taskset_get_tiles(const gpw_taskset *ts, int *tile_z);

@@ -2,7 +2,8 @@
 
 The tiled kernels cut every orthorhombic grid level into tiles of 32 x (128/tz)
 x tz points; tz (4 or 8) trades the number of tiles a cube touches against
-the per-tile work of a pair.  ``gpw_taskset_autotune`` times one collocate +
+the per-tile work of a pair.  On general-cell levels tz = 0 (no tiles: the
+float-float kernel, one CTA per pair) is a third candidate.  ``gpw_taskset_autotune`` times one collocate +
 integrate per candidate and level on the device.  This module keys the result
 by a workload signature (grid levels and the task set's size, angular momentum
 and exponent spread) and keeps it in a JSON table, so a task set of the same
@@ -72,7 +73,7 @@ def apply(ts, pab, tasks=None, path: str | None = None, tune: bool = True) -> tu
     if not tune:
         return ts.tiles(), "default"
     tz, ms = ts.autotune(pab)
-    table[key] = {"tile_z": tz, "ms": [[round(float(v), 3) for v in row] for row in ms], "candidates_tz": [8, 4]}
+    table[key] = {"tile_z": tz, "ms": [[round(float(v), 3) for v in row] for row in ms], "candidates_tz": [8, 4, 0]}
     try:
         save_table(table, path)
     except OSError:

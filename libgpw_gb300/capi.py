@@ -202,7 +202,8 @@ class TaskSet:
     def check(self, stream=None):
         check(lib().gpw_taskset_check(self.handle, _stream_handle(stream)), "device status")
 
-    # tile shapes of the mixed path (z extent per level: 4 or 8)
+    # tile shapes of the mixed path (z extent per level: 4 or 8; 0 = a general-cell
+    # level on the float-float kernel instead of tiles)
     def set_tiles(self, tile_z):
         tz = np.ascontiguousarray(np.asarray(tile_z, dtype=np.int32).reshape(-1))
         assert tz.size == len(self.plan.levels)
@@ -215,13 +216,13 @@ class TaskSet:
 
     def autotune(self, pab, stream=None) -> tuple:
         """Times each tile shape (gpw_taskset_autotune) and keeps the fastest:
-        (tile z per level, ms[level][candidate tz = 8, 4])."""
+        (tile z per level, ms[level][candidate tz = 8, 4, 0]; 0 only on general-cell levels)."""
         nl = len(self.plan.levels)
         tz = np.zeros(nl, np.int32)
-        ms = np.zeros(2 * nl, np.float64)
+        ms = np.zeros(3 * nl, np.float64)
         check(lib().gpw_taskset_autotune(self.handle, pab.data_ptr(), tz.ctypes.data, ms.ctypes.data,
                                          _stream_handle(stream)), "gpw_taskset_autotune")
-        return [int(v) for v in tz], ms.reshape(nl, 2)
+        return [int(v) for v in tz], ms.reshape(nl, 3)
 
     # host-buffer calls (numpy in, numpy out; copies inside the library)
     def collocate_host(self, pab: np.ndarray, grids: list, precision: str = "fp64"):

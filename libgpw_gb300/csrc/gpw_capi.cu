@@ -431,7 +431,8 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
     });
     gpw_taskset *T = new gpw_taskset();
     T->plan = plan;
-    for (int l = 0; l < GPW_MAX_LEVELS; l++) T->tile_lz[l] = kDefaultTileLz;
+    for (int l = 0; l < GPW_MAX_LEVELS; l++)  // general-cell levels start on the float-float kernel
+        T->tile_lz[l] = (l < plan->nlevels && !plan->lv[l].ortho) ? kUntiled : kDefaultTileLz;
     T->tau = compute_tau ? 1 : 0;
     T->ntasks = ntasks;
     T->pab_extent = extent;
@@ -616,7 +617,9 @@ int gpw_taskset_check(gpw_taskset *ts, void *stream) {
     return GPW_SUCCESS;
 }
 
-static int tile_lz_of(int tz) { return tz == 4 ? 2 : tz == 8 ? 3 : -1; }
+// tz 4 / 8: tiles of that z extent; 0 (general-cell levels only): no tiles, the float-float kernel
+static int tile_lz_of(int tz, bool ortho) { return tz == 4 ? 2 : tz == 8 ? 3 : (tz == 0 && !ortho) ? kUntiled : -2; }
+static int tile_z_of(int lz) { return lz == kUntiled ? 0 : 1 << lz; }
 
 static int retile(gpw_taskset *ts, const int *lz) {
     bool same = true;
@@ -636,15 +639,17 @@ int gpw_taskset_set_tiles(gpw_taskset *ts, const int *tile_z) {
     if (!ts || !tile_z) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_set_tiles: null");
     int lz[GPW_MAX_LEVELS];
     for (int l = 0; l < ts->plan->nlevels; l++) {
-        lz[l] = tile_lz_of(tile_z[l]);
-        if (lz[l] < 0) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_set_tiles: tile z extent must be 4 or 8");
+        lz[l] = tile_lz_of(tile_z[l], ts->plan->lv[l].ortho != 0);
+        if (lz[l] == -2)
+            return fail(GPW_ERR_INVALID_ARG,
+                        "gpw_taskset_set_tiles: tile z extent must be 4 or 8 (or 0 on a general-cell level)");
     }
     return retile(ts, lz);
 }
 
 int gpw_taskset_get_tiles(const gpw_taskset *ts, int *tile_z) {
     if (!ts || !tile_z) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_get_tiles: null");
-    for (int l = 0; l < ts->plan->nlevels; l++) tile_z[l] = 1 << ts->tile_lz[l];
+    for (int l = 0; l < ts->plan->nlevels; l++) tile_z[l] = tile_z_of(ts->tile_lz[l]);
     return GPW_SUCCESS;
 }
 
@@ -665,7 +670,7 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
     if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
     if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
     int st = ce == cudaSuccess ? GPW_SUCCESS : cuda_fail(ce, "gpw_taskset_autotune");
-    static const int cand[2] = {3, 2};  // TZ = 8, 4
+    static const int cand[3] = {3, 2, kUntiled};  // TZ = 8, 4; general-cell levels also untiled
     int best[GPW_MAX_LEVELS];
     for (int l = 0; l < P.nlevels; l++) best[l] = ts->tile_lz[l];
     auto time_once = [&](float &out) -> int {
@@ -682,12 +687,13 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
         return GPW_SUCCESS;
     };
     for (int l = 0; l < P.nlevels && !st; l++) {
-        bool used = false;  // levels without orthorhombic tasks keep their shape
-        for (int64_t k = 0; k < ts->ntasks && !used; k++) used = ts->h_geom[k].ortho && ts->h_geom[k].level == l;
+        bool used = false;  // levels without tasks keep their shape
+        for (int64_t k = 0; k < ts->ntasks && !used; k++) used = ts->h_geom[k].level == l;
+        const int ncand = P.lv[l].ortho ? 2 : 3;
         float best_ms = -1.0f;
-        for (int c = 0; c < 2 && !st; c++) {
+        for (int c = 0; c < 3 && !st; c++) {
             float t = 0.0f;
-            if (used) {
+            if (used && c < ncand) {
                 int lz[GPW_MAX_LEVELS];
                 for (int j = 0; j < P.nlevels; j++) lz[j] = best[j];
                 lz[l] = cand[c];
@@ -695,13 +701,13 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
                 if (!st) st = time_once(t);
                 if (!st && (best_ms < 0.0f || t < best_ms)) best_ms = t, best[l] = cand[c];
             }
-            if (ms) ms[2 * l + c] = used ? (double)t : -1.0;
+            if (ms) ms[3 * l + c] = (used && c < ncand) ? (double)t : -1.0;
         }
     }
     if (!st) st = retile(ts, best);
     if (!st) st = gpw_taskset_check(ts, stream);
     if (tile_z)
-        for (int l = 0; l < P.nlevels; l++) tile_z[l] = 1 << ts->tile_lz[l];
+        for (int l = 0; l < P.nlevels; l++) tile_z[l] = tile_z_of(ts->tile_lz[l]);
     for (int l = 0; l < P.nlevels; l++) cudaFree(grids[l]);
     cudaFree(hab);
     if (e0) cudaEventDestroy(e0);

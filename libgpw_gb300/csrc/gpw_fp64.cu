@@ -291,28 +291,7 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
 }
 
 // ---------------------------------------------------------------------------
-// general cell, one CTA per pair: rows of the index box, i-range from the
-// quadratic |i h0 + v|^2 <= r^2 (grid_base_ref_c.cc:781-807)
-GPW_HD bool general_row(const double dh[3][3], const double gp[3], double dj, double dk,
-                        double radius, int &ismin, int &ismax) {
-    double a = 0.0, b = 0.0, c = 0.0;
-    for (int i = 0; i < 3; i++) {
-        const double pointk = rmul(dh[2][i], dk);
-        const double pointj = radd(pointk, rmul(dh[1][i], dj));
-        const double v = rsub(pointj, rmul(gp[0], dh[0][i]));
-        a = radd(a, rmul(dh[0][i], dh[0][i]));
-        b = radd(b, rmul(rmul(2.0, v), dh[0][i]));
-        c = radd(c, rmul(v, v));
-    }
-    double d = rsub(rmul(b, b), rmul(rmul(4.0, a), rsub(c, rmul(radius, radius))));
-    if (d < 0.0) return false;
-    d = rsqrt_rn(d);
-    const double a2 = rmul(2.0, a);
-    ismin = (int)ceil(rdiv(rsub(-b, d), a2));
-    ismax = (int)floor(rdiv(radd(-b, d), a2));
-    return true;
-}
-
+// general cell, one CTA per pair (row bounds: general_row, gpw_common.cuh)
 int smem_general_fp64(const PairGeom &g, int extra) {
     const int L = g.lp + 1 + extra;
     const int ny = g.hi[1] - g.cc[1] + 1;

@@ -33,6 +33,7 @@ struct Plan {
 
 struct MixedState;  // tiled path, gpw_mixed.cu
 constexpr int kDefaultTileLz = 3;  // tiles of 32 x 16 x 8 points until set or tuned
+constexpr int kUntiled = -1;       // a general-cell level on the float-float kernel
 
 struct TaskSet {
     Plan *plan = nullptr;

@@ -67,7 +67,7 @@ struct TileShape {
 // pair data a tile needs, staged in shared memory
 struct TPair {
     double r2;          // radius^2 (FP64, rule decisions)
-    double hz, hy, hx;
+    double hz, hy, hx;  // spacings (orthorhombic rule); general cell: 1 / |v_2|, 1 / |v_1|, 1 / |v_0|
     float r2f, hzf, hyf, hxf;
     float hyinvf, hxinvf;  // 1/hy, 1/hx rounded to float
     ff zetp;
@@ -75,7 +75,17 @@ struct TPair {
     ff h[3];
     int lb[3], hi[3], cc[3];
     int kgmin, lp, L;
+    int general, pad_;  // general cell: box-relative cube (lb = 0), lattice-step lengths in h
     int64_t coef_off, table_off;
+    double gp[3];       // general: the product centre in lattice coordinates (dh_inv^T rp)
+    double radius;      // general: the cube radius (the row rule squares it itself)
+};
+// General-cell level constants of the tiled path: FP32 lattice steps for the row
+// rule, and the cosines between the steps (cross terms of the Gaussian).
+struct GenLevel {
+    float dh[3][3];
+    float a, inv2a;     // |v0|^2 and 1 / (2 |v0|^2)
+    ff c01, c02, c12;   // cos(v0, v1), cos(v0, v2), cos(v1, v2)
 };
 // A pair's blob: the record padded to kHdr16 16-byte chunks, then its
 // coefficients as float-float (written by every collocate call), padded to 16 bytes.
@@ -111,10 +121,15 @@ struct MixedState {
     int64_t *d_start = nullptr;    // ntiles + 1
     uint64_t *d_items = nullptr;   // per (tile, pair): blob offset << 16 | chunks
     ItemImg *d_iimg = nullptr;     // per (tile, pair): images
-    int *d_queue = nullptr;      // [0]: collocate, [1]: integrate
+    int *d_queue = nullptr;      // [0]: collocate, [1]: integrate (orthorhombic tiles), [2], [3]: general tiles
+    GenLevel *d_glv = nullptr;   // per level (general levels only meaningful)
     int northo = 0;              // ortho tasks come first in sorted order
+    int64_t nbin = 0;            // tasks [0, nbin) are binned (the ortho ones, then general ones if tiled)
+    bool gen_tiled = false;      // general-cell pairs run on the tiled kernels
+    int ntiles_ortho = 0;        // tiles [0, ntiles_ortho) are orthorhombic, the rest general
     int grid_ctas = 0;    // collocate
     int grid_ctas_i = 0;  // integrate
+    int sms = 0;
     int per_sm = 0, per_sm_i = 0;
 };
 
@@ -182,6 +197,73 @@ __device__ __forceinline__ void row_range(const TPair &p, const ImgState &q, con
     x1 = min(1 - imin - q.o[0], q.gx1);
 }
 
+// General cell: the row (jj, kk) of the index box holds the points i with
+// |i v0 + w|^2 <= r^2 (the reference's quadratic, grid_base_ref_c.cc:781-807).
+// FP32 estimate in box-relative units i' = i - cc0 with a running error bound;
+// the exact FP64 rule (general_row, gpw_common.cuh) decides where a root lies
+// within its bound of an integer or the discriminant within its bound of zero.
+__device__ __noinline__ bool general_row_exact(const LevelDev &lv, const TPair &p, int jj, int kk, int &ismin,
+                                               int &ismax) {
+    const double dj = rsub((double)jj, p.gp[1]), dk = rsub((double)kk, p.gp[2]);
+    return general_row(lv.dh, p.gp, dj, dk, p.radius, ismin, ismax);
+}
+
+__device__ __forceinline__ bool general_row_fast(const LevelDev &lv, const GenLevel &G, const TPair &p, int jj,
+                                                 int kk, int &ismin, int &ismax) {
+    const float eps = 1.2e-7f;  // 2^-23, with room
+    const float gj = (float)(p.gp[1] - (double)p.cc[1]), gk = (float)(p.gp[2] - (double)p.cc[2]);
+    const float gi = (float)(p.gp[0] - (double)p.cc[0]);
+    const float dj = (float)(jj - p.cc[1]) - gj, dk = (float)(kk - p.cc[2]) - gk;
+    float b = 0.0f, c = 0.0f, eb = 0.0f, ec = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        // v_i = dk dh2_i + dj dh1_i - gi dh0_i (box-relative), with its error bound
+        const float v = __fsub_rn(__fadd_rn(__fmul_rn(G.dh[2][i], dk), __fmul_rn(G.dh[1][i], dj)),
+                                  __fmul_rn(gi, G.dh[0][i]));
+        const float ev = eps * (fabsf(G.dh[2][i]) * (2.0f * fabsf(dk) + fabsf(gk)) +
+                                fabsf(G.dh[1][i]) * (2.0f * fabsf(dj) + fabsf(gj)) +
+                                2.0f * fabsf(gi * G.dh[0][i]) + 2.0f * fabsf(v));
+        b = __fadd_rn(b, __fmul_rn(2.0f * v, G.dh[0][i]));
+        c = __fadd_rn(c, __fmul_rn(v, v));
+        eb += 2.0f * ev * fabsf(G.dh[0][i]) + 2.0f * eps * fabsf(b);
+        ec += (2.0f * fabsf(v) + ev) * ev + 2.0f * eps * c;
+    }
+    // d = b^2 - 4a(c - r^2): propagated input errors, the representation errors of
+    // a and r^2, and the rounding of each operation
+    const float a = G.a, r2 = p.r2f;
+    const float cr = __fsub_rn(c, r2);
+    const float d = __fsub_rn(__fmul_rn(b, b), __fmul_rn(4.0f * a, cr));
+    const float ed = 2.0f * fabsf(b) * eb + eb * eb + eps * b * b +
+                     4.0f * a * (ec + eps * r2 + 2.5f * eps * fabsf(cr)) + eps * fabsf(d);
+    bool unsure = fabsf(d) <= 1.5f * ed;
+    if (!unsure && d < 0.0f) return false;  // surely empty
+    if (!unsure) {
+        const float sd = sqrtf(d);
+        const float esd = 1.8f * ed / sd + eps * sd;  // d > 1.5 ed: sqrt(d - ed) >= sd / sqrt(3)
+        const float lo = __fmul_rn(__fsub_rn(-b, sd), G.inv2a), hi = __fmul_rn(__fadd_rn(-b, sd), G.inv2a);
+        const float er = 1.25f * ((eb + esd + eps * (fabsf(b) + sd)) * G.inv2a + 1.5f * eps * (fabsf(lo) + fabsf(hi))) +
+                         1e-6f;
+        unsure = fabsf(lo - rintf(lo)) <= er || fabsf(hi - rintf(hi)) <= er;
+        ismin = p.cc[0] + (int)ceilf(lo);
+        ismax = p.cc[0] + (int)floorf(hi);
+    }
+    if (unsure) return general_row_exact(lv, p, jj, kk, ismin, ismax);
+    return true;
+}
+
+// Row (z, y) of the tile for a general-cell pair: tile-local x range [x0, x1].
+__device__ __forceinline__ void general_row_range(const LevelDev &lv, const GenLevel &G, const TPair &p,
+                                                  const ImgState &q, int gz, int gy, int ext_ok, int &x0,
+                                                  int &x1) {
+    x0 = 1;
+    x1 = 0;
+    if (!ext_ok || gz < 0 || gz > p.hi[2] || gy < 0 || gy > p.hi[1]) return;
+    int ismin, ismax;
+    if (!general_row_fast(lv, G, p, p.cc[1] + gy, p.cc[2] + gz, ismin, ismax)) return;
+    x0 = max(ismin - p.cc[0] - q.o[0], q.gx0);
+    x1 = min(ismax - p.cc[0] - q.o[0], q.gx1);
+}
+
 // UMMA canonical K-major layout, no swizzle: core matrices of 8 rows x 16 bytes
 // (8 halves of K).  Element (row r, k) of an operand with R rows, K = 16:
 //   byte offset = (r / 8) * SBO + (k / 8) * LBO + (r % 8) * 16 + (k % 8) * 2,
@@ -229,6 +311,7 @@ struct MixedArgs {
     const uint64_t *items;    // per (tile, pair): blob offset in 16-byte chunks << 16 | chunks to copy
     const ItemImg *iimg;      // per (tile, pair): images
     const int *table;
+    const GenLevel *glv;  // general levels: FP32 steps, cosines
     double *mom;  // integrate: per-pair moments
     GridPtrs grids;
     int *queue;
@@ -293,7 +376,11 @@ struct alignas(128) SmemInt {
         __half B[2][NSL][KP * KP];        // X' slices, N=16 (alpha) x K=16 per half
         float xmax[kNPow][TX + 4];        // |X[alpha][x]| for the per-alpha maxima, before B is written
     };
-    __half Vs[2][NSL][MROWS * KP];  // this tile's V slices, unmasked, in the layout of A
+    union {
+        __half Vs[2][NSL][MROWS * KP];  // this tile's V slices, unmasked, in the layout of A
+        ff Vff[TX][MROWS];              // general cell: this tile's V (x-major: lanes read consecutive rows)
+    };
+    int vmr[MROWS];  // general cell: each row's exponent of V E in the current image
     int gexp[KP];
     signed char rx0[MROWS], rx1[MROWS];  // each row's cube x range in the current image
     PairHdr pb[2];                       // the current pair's record and the one being fetched
@@ -539,6 +626,84 @@ __device__ __forceinline__ void slice_row16(const ff *v, float sc, int kw, __hal
 __device__ __forceinline__ void bar_arrive1(int n) { asm volatile("bar.arrive 1, %0;" ::"r"(n) : "memory"); }
 __device__ __forceinline__ void bar_sync1(int n) { asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); }
 
+// General cell: the cross factor along row (z, y) of the current image, E(x) =
+// exp(alpha + beta t0(x)) with beta = -2 zetp (c01 t1 + c02 t2), alpha = -2 zetp
+// c12 t1 t2: returns E(x0) and q = E(x + 1) / E(x).
+__device__ __forceinline__ void cross_factor_row(const GenLevel &G, const TPair &P, const ImgState &Q, int z, int y,
+                                                 int x0, ff &e0, ff &q) {
+    const ff t1 = ff_add(ff_mul_f(P.h[1], (float)(Q.o[1] + y)), ff{-P.off[1].hi, -P.off[1].lo});
+    const ff t2 = ff_add(ff_mul_f(P.h[2], (float)(Q.o[2] + z)), ff{-P.off[2].hi, -P.off[2].lo});
+    const ff t0 = ff_add(ff_mul_f(P.h[0], (float)(Q.o[0] + x0)), ff{-P.off[0].hi, -P.off[0].lo});
+    const ff m2z = {-2.0f * P.zetp.hi, -2.0f * P.zetp.lo};
+    const ff beta = ff_mul(m2z, ff_add(ff_mul(G.c01, t1), ff_mul(G.c02, t2)));
+    const ff alpha = ff_mul(m2z, ff_mul(G.c12, ff_mul(t1, t2)));
+    e0 = ff_exp(ff_add(alpha, ff_mul(beta, t0)));
+    q = ff_exp(ff_mul(beta, P.h[0]));
+}
+
+// General cell, integrate: the A operand row r = the slices of V(x) E(x) over the
+// row's cube points (zero elsewhere), with the row's own exponent (vmr[r]).
+template <class Smem>
+__device__ __forceinline__ void general_a_row(Smem &sm, const GenLevel &G, const TPair &P, const ImgState &Q,
+                                              const TileShape &sh, int r, bool &zero_row) {
+    const int x0 = sm.rx0[r], x1 = sm.rx1[r];
+    if (x0 > x1) {
+        sm.vmr[r] = kZeroExp;
+        if (zero_row) return;
+        zero_row = true;
+#pragma unroll
+        for (int v = 0; v < TX / 8; v++)
+#pragma unroll
+            for (int q = 0; q < NSL; q++)
+                reinterpret_cast<uint4 *>(sm.A[v >> 1][q])[(r >> 3) * 16 + (v & 1) * 8 + (r & 7)] = make_uint4(0, 0, 0, 0);
+        return;
+    }
+    zero_row = false;
+    ff e0, q;
+    cross_factor_row(G, P, Q, r >> sh.ly, r & (sh.TY - 1), x0, e0, q);
+    // pass 1: the row maximum of |V E|
+    float mx = 0.0f;
+    {
+        ff e = e0;
+        for (int x = x0; x <= x1; x++) {
+            mx = fmaxf(mx, fabsf(ff_mul(sm.Vff[x][r], e).hi));
+            e = ff_mul(e, q);
+        }
+    }
+    const int vmx = exp_of(mx);
+    sm.vmr[r] = vmx;
+    const float sc = vmx == kZeroExp ? 0.0f : pow2i(SLB - vmx);
+    // pass 2: slices, 16-byte chunks of 8 x
+    ff e = e0;
+#pragma unroll 1
+    for (int c = 0; c < TX / 8; c++) {
+        uint32_t w[NSL][4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            ff v2[2];
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int x = 8 * c + 2 * i + h;
+                const bool in = x >= x0 && x <= x1;
+                v2[h] = in ? ff_mul(sm.Vff[x][r], e) : ff{0.0f, 0.0f};
+                if (in) e = ff_mul(e, q);
+            }
+            float s0[NSL], s1[NSL];
+            slice_scaled(v2[0], sc, s0);
+            slice_scaled(v2[1], sc, s1);
+#pragma unroll
+            for (int qq = 0; qq < NSL; qq++) {
+                const __half2 h2 = __floats2half2_rn(s0[qq], s1[qq]);
+                w[qq][i] = *reinterpret_cast<const uint32_t *>(&h2);
+            }
+        }
+        const int o16 = (r >> 3) * 16 + (c & 1) * 8 + (r & 7);
+#pragma unroll
+        for (int qq = 0; qq < NSL; qq++)
+            reinterpret_cast<uint4 *>(sm.A[c >> 1][qq])[o16] = make_uint4(w[qq][0], w[qq][1], w[qq][2], w[qq][3]);
+    }
+}
+
 // TMEM set-up shared by both kernels: warp 0 allocates, thread 0 inits the mbarrier
 __device__ __forceinline__ void tc_setup(TileCommon &c, uint32_t ncols) {
     if (threadIdx.x == 0) {
@@ -615,6 +780,15 @@ __device__ __forceinline__ int item_images(TileCommon &cm, const ItemImg &ii, co
 constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
+// kGeneral: tiles of general-cell levels.  The tables, stages and slices are the
+// same in t_d = (index_d - gp_d) |v_d|; the row ranges come from the quadratic
+// rule, and every point's value is multiplied by the cross factor
+// E = exp(-2 zetp (c01 t0 t1 + c02 t0 t2 + c12 t1 t2)) of the Gaussian
+// (exp(-zetp |r|^2) = exp(-zetp (t0^2 + t1^2 + t2^2)) E).  Along a row E(x) is
+// exp(alpha + beta t0(x)): one exp at the row's first cube point, then E(x+1) =
+// E(x) q, q = exp(beta |v0|), over the row's cube points only (so no intermediate
+// leaves the range of the factor inside the cube).
+template <bool kGeneral>
 __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemColl &sm = *reinterpret_cast<SmemColl *>(smraw);
@@ -713,7 +887,11 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 __syncthreads();
                 // stage 2 (this thread's row, all a at once) + culling + A slices
                 int x0, x1;
-                row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
+                if constexpr (kGeneral)
+                    general_row_range(lv, A.glv[td.level], P, Q, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0,
+                                      x1);
+                else
+                    row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
                 ff cx[kNPow];
 #pragma unroll
                 for (int a = 0; a < kNPow; a++) cx[a] = ff{0.0f, 0.0f};
@@ -777,6 +955,11 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 phase ^= 1u;
                 if (!ok) break;
                 if (tid == 0) cm.kmax = L;  // read again only after the next barrier
+                // cross factor of the general cell along this row: E0 at x0, ratio q
+                ff ecur = {1.0f, 0.0f}, eq = {1.0f, 0.0f};
+                if constexpr (kGeneral) {
+                    if (x0 <= x1) cross_factor_row(A.glv[td.level], P, Q, z, y, x0, ecur, eq);
+                }
                 // tcgen05.ld is warp-collective: chunk decisions are made per warp
                 if (__any_sync(0xffffffffu, x0 <= x1)) {
                     const float rs = pow2i(max(em - 2 * SLB, -126));
@@ -806,8 +989,14 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                                                          __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
                             const float scl = __fmul_rn(rs, csv[i]);
                             const float h0 = __fadd_rn(d2, corr);
-                            const float hi = __fmul_rn(h0, scl);
-                            const float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
+                            float hi = __fmul_rn(h0, scl);
+                            float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
+                            if constexpr (kGeneral) {
+                                if (x > x0) ecur = ff_mul(ecur, eq);  // E(x) on the row's cube points
+                                const ff v = ff_mul(ff{hi, lo}, ecur);
+                                hi = v.hi;
+                                lo = v.lo;
+                            }
                             const float sv = __fadd_rn(acc_hi[x], hi);
                             const float bb = __fsub_rn(sv, acc_hi[x]);
                             const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
@@ -836,6 +1025,10 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     tc_teardown(cm, kCols, phase);
 }
 
+// kGeneral: tiles of general-cell levels; the A operand holds the slices of
+// V(x) E(x) (E the cross factor of the Gaussian along the row), one row per
+// thread, with its own exponent per row and image.
+template <bool kGeneral>
 __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
     SmemInt &sm = *reinterpret_cast<SmemInt *>(smraw);
@@ -871,13 +1064,17 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
             ff v[TX];
 #pragma unroll
             for (int x = 0; x < TX; x++) v[x] = (ok && x < ext_x) ? ff_from_double(grid[row + x]) : ff{0.0f, 0.0f};
+            if constexpr (kGeneral) {
+#pragma unroll
+                for (int x = 0; x < TX; x++) sm.Vff[x][m] = v[x];
+            }
             float mx = 0.0f;
 #pragma unroll
             for (int x = 0; x < TX; x++) mx = fmaxf(mx, fabsf(v[x].hi));
             vm = exp_of(mx);
             const float sc = vm == kZeroExp ? 0.0f : pow2i(SLB - vm);
 #pragma unroll
-            for (int c = 0; c < TX / 8; c++) {  // 8 x per 16-byte chunk of the UMMA layout
+            for (int c = 0; c < TX / 8 && !kGeneral; c++) {  // 8 x per 16-byte chunk of the UMMA layout
                 uint32_t w[NSL][4];
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
@@ -921,13 +1118,17 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                 {
                     // every thread: its row's cube x range, for the A operand of warps 2-3
                     int x0, x1;
-                    row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
+                    if constexpr (kGeneral)
+                        general_row_range(lv, A.glv[td.level], P, Q, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y,
+                                          x0, x1);
+                    else
+                        row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
                     const bool empty = x0 > x1;  // otherwise both lie in [0, TX)
                     sm.rx0[m] = (signed char)(empty ? 1 : x0);
                     sm.rx1[m] = (signed char)(empty ? 0 : x1);
                 }
                 if (warp == 0) {
-                    bar_arrive1(NTHR);
+                    if constexpr (!kGeneral) bar_arrive1(NTHR);
                     // X column (lane x) in registers, then B: row alpha = X[alpha][x] over x,
                     // scaled by 2^(SLB - gexp[alpha]) (maximum over the warp); rows alpha >= L
                     // are left as they are (their output columns are not read)
@@ -960,9 +1161,9 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                         for (int q = 0; q < NSL; q++) sm.B[h][q][o] = __float2half_rn(sl[q]);
                     }
                 } else if (warp == 1) {
-                    bar_arrive1(NTHR);
+                    if constexpr (!kGeneral) bar_arrive1(NTHR);
                     build_yz(cm, P, Q, lv, td);
-                } else {
+                } else if constexpr (!kGeneral) {
                     bar_sync1(NTHR);
                     // A operand: V slices of rows u and u + 64 masked to the rows' cube ranges,
                     // 16-byte chunks (8 x of one K half); rows already zero stay untouched
@@ -999,6 +1200,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                         }
                     }
                 }
+                if constexpr (kGeneral) general_a_row(sm, A.glv[td.level], P, Q, sh, m, zero_row[0]);
                 tc::fence_async_smem();
                 tc::fence_before_sync();
                 __syncthreads();
@@ -1050,8 +1252,9 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                             t.lo = __fadd_rn(t.lo, __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
                                                              __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f, d2.lo)));
                             t = fast_two_sum(t.hi, t.lo);
-                            const int E = vm + sm.gexp[a] - 2 * SLB;
-                            if (E >= -126 && vm != kZeroExp && sm.gexp[a] != kZeroExp) {
+                            const int vrow = kGeneral ? sm.vmr[m] : vm;
+                            const int E = vrow + sm.gexp[a] - 2 * SLB;
+                            if (E >= -126 && vrow != kZeroExp && sm.gexp[a] != kZeroExp) {
                                 const float scl = pow2i(min(E, 127));
                                 s = {__fmul_rn(t.hi, scl), __fmul_rn(t.lo, scl)};
                             }
@@ -1102,7 +1305,16 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                         s1 = ff_fma(sm.st.T[zz + 1][pi], cm.Z[g][zz + 1], s1);
                     }
                     const ff s = ff_add(s0, s1);
-                    if (s.hi != 0.0f) atomicAdd(A.mom + moff + t, (double)s.hi + (double)s.lo);
+                    if (s.hi != 0.0f) {
+                        double val = (double)s.hi + (double)s.lo;
+                        if constexpr (kGeneral) {
+                            // moments in powers of t_d = d_d |v_d| -> lattice-index powers d_d
+                            for (int e = 0; e < a; e++) val *= P.hx;
+                            for (int e = 0; e < b; e++) val *= P.hy;
+                            for (int e = 0; e < g; e++) val *= P.hz;
+                        }
+                        atomicAdd(A.mom + moff + t, val);
+                    }
                 }
                 __syncthreads();
             }
@@ -1121,10 +1333,30 @@ __global__ void k_coef_to_blob(const double *__restrict__ c, uint4 *blob, const 
     for (int64_t k = blockIdx.x * (int64_t)(blockDim.x >> 5) + (threadIdx.x >> 5); k < ntask; k += nw) {
         const TPair *p = reinterpret_cast<const TPair *>(blob + off16[k]);
         const int64_t src = p->coef_off;
-        const int nc = ncoef(p->lp);
+        const int lp = p->lp;
+        const int nc = ncoef(lp);
         float2 *dst = reinterpret_cast<float2 *>(blob + off16[k] + kHdr16);
+        // general cell: lattice-index powers di^a dj^b dk^g -> powers of t_d = d_d |v_d|
+        double hinv[3] = {1.0, 1.0, 1.0};
+        if (p->general)
+            for (int d = 0; d < 3; d++) hinv[d] = 1.0 / ((double)p->h[d].hi + (double)p->h[d].lo);
         for (int t = lane; t < nc; t += 32) {
-            const double d = c[src + t];
+            double d = c[src + t];
+            if (p->general) {
+                int g = 0, b = 0, r = t;
+                for (g = 0; g <= lp; g++) {
+                    const int cnt = ((lp - g + 1) * (lp - g + 2)) / 2;
+                    if (r < cnt) break;
+                    r -= cnt;
+                }
+                for (b = 0; b <= lp - g; b++) {
+                    if (r <= lp - g - b) break;
+                    r -= lp - g - b + 1;
+                }
+                for (int e = 0; e < g; e++) d *= hinv[2];
+                for (int e = 0; e < b; e++) d *= hinv[1];
+                for (int e = 0; e < r; e++) d *= hinv[0];
+            }
             const float h = __double2float_rn(d);
             dst[t] = make_float2(h, __double2float_rn(d - (double)h));
         }
@@ -1204,12 +1436,69 @@ int mixed_build(TaskSet &ts, std::string &err) {
     int64_t northo = 0;
     while (northo < ts.ntasks && ts.h_geom[northo].ortho) northo++;
     M->northo = (int)northo;
-    // tiles of every orthorhombic level
+    // General-cell levels go on the tiled kernels when the cosine matrix C of the
+    // lattice steps satisfies C >= 0.4 I: then sum t_d^2 <= 2.5 r^2, so inside the
+    // cube the cross factor exp(-2 zetp sum c_de t_d t_e) of the Gaussian stays
+    // within exp(+-58) (float range).  Otherwise they stay on the float-float
+    // general kernel.
+    std::vector<GenLevel> glv(P.nlevels);
+    bool gen_ok = true;
+    for (int l = 0; l < P.nlevels; l++) {
+        const LevelDev &lv = P.lv[l];
+        if (lv.ortho) continue;
+        double G[3][3], h[3];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                G[a][b] = lv.dh[a][0] * lv.dh[b][0] + lv.dh[a][1] * lv.dh[b][1] + lv.dh[a][2] * lv.dh[b][2];
+        for (int a = 0; a < 3; a++) h[a] = std::sqrt(G[a][a]);
+        double C[3][3];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) C[a][b] = G[a][b] / (h[a] * h[b]) - (a == b ? 0.4 : 0.0);
+        const double m1 = C[0][0], m2 = C[0][0] * C[1][1] - C[0][1] * C[1][0];
+        const double m3 = C[0][0] * (C[1][1] * C[2][2] - C[1][2] * C[2][1]) -
+                          C[0][1] * (C[1][0] * C[2][2] - C[1][2] * C[2][0]) +
+                          C[0][2] * (C[1][0] * C[2][1] - C[1][1] * C[2][0]);
+        if (!(m1 > 0.0 && m2 > 0.0 && m3 > 0.0)) gen_ok = false;
+        GenLevel &q = glv[l];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) q.dh[a][b] = (float)lv.dh[a][b];
+        q.a = (float)G[0][0];
+        q.inv2a = (float)(0.5 / G[0][0]);
+        auto sp = [](double d) {
+            const float hi = (float)d;
+            return ff{hi, (float)(d - (double)hi)};
+        };
+        q.c01 = sp(G[0][1] / (h[0] * h[1]));
+        q.c02 = sp(G[0][2] / (h[0] * h[2]));
+        q.c12 = sp(G[1][2] / (h[1] * h[2]));
+    }
+    const int64_t ngen = ts.ntasks - northo;
+    // ... when every general level has a tile shape (not kUntiled) ...
+    for (int l = 0; l < P.nlevels; l++)
+        if (!P.lv[l].ortho && ts.tile_lz[l] == kUntiled) gen_ok = false;
+    // ... and when no general box spans more periodic images of one tile axis
+    // than the kernels hold (kMaxImages): count <= (extent + T - 1) / N + 1
+    for (int64_t k = northo; k < ts.ntasks && gen_ok; k++) {
+        const PairGeom &g = ts.h_geom[k];
+        const LevelDev &lv = P.lv[g.level];
+        const TileShape sh(ts.tile_lz[g.level]);
+        const int T[3] = {TX, sh.TY, sh.TZ};
+        for (int d = 0; d < 3; d++)
+            if (lv.periodic[d] && (g.hi[d] - g.cc[d] + 1) + T[d] - 1 > (kMaxImages - 1) * lv.npts[d]) gen_ok = false;
+    }
+    M->gen_tiled = gen_ok && ngen > 0;
+    const int64_t nbin = northo + (M->gen_tiled ? ngen : 0);
+    M->nbin = nbin;
+    std::vector<char> binned_level(P.nlevels, 0);
+    for (int64_t k = 0; k < nbin; k++) binned_level[ts.h_geom[k].level] = 1;
+    // tiles of every level with binned pairs: orthorhombic levels first
     std::vector<int> lvl_first(P.nlevels, -1);
     std::vector<TileDesc> tiles;
     int ntx[GPW_MAX_LEVELS], nty[GPW_MAX_LEVELS], ntz[GPW_MAX_LEVELS];
+    for (int pass = 0; pass < 2; pass++)
     for (int l = 0; l < P.nlevels; l++) {
-        if (!P.lv[l].ortho) continue;
+        if ((pass == 0) != (P.lv[l].ortho != 0)) continue;
+        if (!P.lv[l].ortho && !binned_level[l]) continue;
         ntx[l] = (P.lv[l].ngrid[0] + TX - 1) / TX;
         const TileShape sh(ts.tile_lz[l]);
         nty[l] = (P.lv[l].ngrid[1] + sh.TY - 1) / sh.TY;
@@ -1219,15 +1508,24 @@ int mixed_build(TaskSet &ts, std::string &err) {
             for (int b = 0; b < nty[l]; b++)
                 for (int c = 0; c < ntx[l]; c++) tiles.push_back(TileDesc{l, {c, b, a}, ts.tile_lz[l]});
     }
+    int nto = 0;
+    while (nto < (int)tiles.size() && P.lv[tiles[nto].level].ortho) nto++;
+    M->ntiles_ortho = nto;
     const int ntiles = (int)tiles.size();
     std::vector<int64_t> count(ntiles + 1, 0);
     std::vector<AxisTile> ax, ay, az;
     // a pair visits a tile only if some cube point of the tile can be inside its
     // sphere: folded distance of the tile's nearest offsets <= radius (with margin)
     auto each = [&](auto &&fn) {
-        for (int64_t k = 0; k < northo; k++) {
-            const PairGeom &g = ts.h_geom[k];
+        for (int64_t k = 0; k < nbin; k++) {
+            PairGeom g = ts.h_geom[k];
             const LevelDev &lv = P.lv[g.level];
+            if (!g.ortho) {  // the index box as a box-relative cube: offsets [0, hi - cc]
+                for (int d = 0; d < 3; d++) {
+                    g.hi[d] -= g.cc[d];
+                    g.lb[d] = 0;
+                }
+            }
             axis_tiles(lv, 0, g, TX, ax);
             const TileShape sh(ts.tile_lz[g.level]);
             axis_tiles(lv, 1, g, sh.TY, ay);
@@ -1235,7 +1533,7 @@ int mixed_build(TaskSet &ts, std::string &err) {
             const int base = lvl_first[g.level];
             const double r2 = g.radius * g.radius * (1.0 + 1e-9) + 1e-12;
             const double hx = lv.dh[0][0], hy = lv.dh[1][1], hz = lv.dh[2][2];
-            const bool table = g.table_off >= 0;  // explicit cube lists: no culling
+            const bool table = g.table_off >= 0 || !g.ortho;  // cube lists, general boxes: no culling
             for (const AxisTile &c : az) {
                 const double dz = c.fmin * hz;
                 if (!table && dz * dz > r2) continue;
@@ -1255,17 +1553,21 @@ int mixed_build(TaskSet &ts, std::string &err) {
     // order tiles by decreasing work for the persistent queue
     std::vector<int> order(ntiles);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return count[a + 1] > count[b + 1]; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {  // within each group (ortho, general)
+        const bool ga = a >= nto, gb = b >= nto;
+        if (ga != gb) return !ga;
+        return count[a + 1] > count[b + 1];
+    });
     std::vector<int> rank(ntiles);
     for (int i = 0; i < ntiles; i++) rank[order[i]] = i;
     std::vector<int64_t> start(ntiles + 1, 0);
     for (int i = 0; i < ntiles; i++) start[i + 1] = start[i] + count[order[i] + 1];
     const int64_t nitems = start[ntiles];
     // blob layout: per task the record, then its coefficients
-    std::vector<int64_t> off16((size_t)std::max<int64_t>(northo, 1), 0);
-    std::vector<int> len16((size_t)std::max<int64_t>(northo, 1), 0);
+    std::vector<int64_t> off16((size_t)std::max<int64_t>(nbin, 1), 0);
+    std::vector<int> len16((size_t)std::max<int64_t>(nbin, 1), 0);
     int64_t nchunks = 0;
-    for (int64_t k = 0; k < northo; k++) {
+    for (int64_t k = 0; k < nbin; k++) {
         off16[k] = nchunks;
         len16[k] = kHdr16 + (ncoef(ts.h_geom[k].lp) * (int)sizeof(float2) + 15) / 16;
         nchunks += len16[k];
@@ -1281,16 +1583,43 @@ int mixed_build(TaskSet &ts, std::string &err) {
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 16));
     };
-    std::vector<uint4> recs((size_t)std::max<int64_t>(northo, 1) * kHdr16);
+    std::vector<uint4> recs((size_t)std::max<int64_t>(nbin, 1) * kHdr16);
     auto split = [](double d) {
         const float h = (float)d;
         return ff{h, (float)(d - (double)h)};
     };
-    for (int64_t k = 0; k < northo; k++) {
+    for (int64_t k = 0; k < nbin; k++) {
         const PairGeom &g = ts.h_geom[k];
         const LevelDev &lv = P.lv[g.level];
         TPair p;
         memset(&p, 0, sizeof p);
+        if (!g.ortho) {
+            // general cell: t_d = (index_d - gp_d) |v_d|, the box as a cube [0, hi - cc] at cc
+            p.general = 1;
+            p.r2 = rmul(g.radius, g.radius);
+            p.hx = 1.0 / std::sqrt(lv.dh[0][0] * lv.dh[0][0] + lv.dh[0][1] * lv.dh[0][1] + lv.dh[0][2] * lv.dh[0][2]);
+            p.hy = 1.0 / std::sqrt(lv.dh[1][0] * lv.dh[1][0] + lv.dh[1][1] * lv.dh[1][1] + lv.dh[1][2] * lv.dh[1][2]);
+            p.hz = 1.0 / std::sqrt(lv.dh[2][0] * lv.dh[2][0] + lv.dh[2][1] * lv.dh[2][1] + lv.dh[2][2] * lv.dh[2][2]);
+            p.r2f = (float)p.r2;
+            p.radius = g.radius;
+            p.zetp = split(g.zetp);
+            for (int d = 0; d < 3; d++) {
+                const double hd = std::sqrt(lv.dh[d][0] * lv.dh[d][0] + lv.dh[d][1] * lv.dh[d][1] +
+                                            lv.dh[d][2] * lv.dh[d][2]);
+                p.h[d] = split(hd);
+                p.off[d] = split((g.off[d] - (double)g.cc[d]) * hd);
+                p.lb[d] = 0;
+                p.hi[d] = g.hi[d] - g.cc[d];
+                p.cc[d] = g.cc[d];
+                p.gp[d] = g.off[d];
+            }
+            p.lp = g.lp;
+            p.L = g.lp + 1;
+            p.coef_off = g.coef_off;
+            p.table_off = -1;
+            memcpy(&recs[(size_t)k * kHdr16], &p, sizeof p);
+            continue;
+        }
         p.r2 = rmul(g.radius, g.radius);
         p.hx = lv.dh[0][0];
         p.hy = lv.dh[1][1];
@@ -1321,13 +1650,13 @@ int mixed_build(TaskSet &ts, std::string &err) {
     if (e == cudaSuccess) e = cudaMemset(M->d_blob, 0, sizeof(uint4) * (size_t)std::max<int64_t>(nchunks, 1));
     if (e == cudaSuccess)
         e = cudaMemcpy(M->d_blob_off, off16.data(), sizeof(int64_t) * off16.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && northo > 0) {
+    if (e == cudaSuccess && nbin > 0) {
         uint4 *d_recs = nullptr;
         e = cudaMalloc(&d_recs, sizeof(uint4) * recs.size());
         if (e == cudaSuccess) e = cudaMemcpy(d_recs, recs.data(), sizeof(uint4) * recs.size(), cudaMemcpyHostToDevice);
         if (e == cudaSuccess) {
-            k_place_records<<<(unsigned)std::min<int64_t>((northo * kHdr16 + 255) / 256, 8192), 256>>>(
-                d_recs, M->d_blob_off, M->d_blob, northo);
+            k_place_records<<<(unsigned)std::min<int64_t>((nbin * kHdr16 + 255) / 256, 8192), 256>>>(
+                d_recs, M->d_blob_off, M->d_blob, nbin);
             e = cudaGetLastError();
         }
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
@@ -1337,7 +1666,10 @@ int mixed_build(TaskSet &ts, std::string &err) {
     alloc((void **)&M->d_start, sizeof(int64_t) * (ntiles + 1));
     alloc((void **)&M->d_items, sizeof(uint64_t) * items.size());
     alloc((void **)&M->d_iimg, sizeof(ItemImg) * items.size());
-    alloc((void **)&M->d_queue, sizeof(int) * 2);
+    alloc((void **)&M->d_queue, sizeof(int) * 5);  // [4]: status sink of the set-up kernels
+    alloc((void **)&M->d_glv, sizeof(GenLevel) * glv.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(M->d_glv, glv.data(), sizeof(GenLevel) * glv.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && ntiles)
         e = cudaMemcpy(M->d_tiles, tiles_sorted.data(), sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -1345,8 +1677,10 @@ int mixed_build(TaskSet &ts, std::string &err) {
     if (e == cudaSuccess && nitems)
         e = cudaMemcpy(M->d_items, items.data(), sizeof(uint64_t) * nitems, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nitems) {
+        // image overflows are reported by the tiled kernels when they run (a plain
+        // FP64 call on this task set must not see them)
         k_item_images<<<std::min(ntiles, 8192), 128>>>(M->d_tiles, M->d_start, M->d_items, M->d_blob, P.d_levels,
-                                                       M->d_iimg, ntiles, ts.d_status);
+                                                       M->d_iimg, ntiles, M->d_queue + 4);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
@@ -1356,11 +1690,13 @@ int mixed_build(TaskSet &ts, std::string &err) {
     }
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, P.device);
-    e = cudaFuncSetAttribute((const void *)k_collocate_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)sizeof(SmemColl));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute((const void *)k_integrate_tiled, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sizeof(SmemInt));
+    const void *kc[2] = {(const void *)k_collocate_tiled<false>, (const void *)k_collocate_tiled<true>};
+    const void *ki[2] = {(const void *)k_integrate_tiled<false>, (const void *)k_integrate_tiled<true>};
+    for (int v = 0; v < 2 && e == cudaSuccess; v++) {
+        e = cudaFuncSetAttribute(kc[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemColl));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(ki[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemInt));
+    }
     if (e != cudaSuccess) {
         err = std::string("mixed_build: ") + cudaGetErrorString(e);
         return GPW_ERR_CUDA;
@@ -1377,12 +1713,13 @@ int mixed_build(TaskSet &ts, std::string &err) {
         const int by_smem = (int)(smem_sm / (dyn + fa.sharedSizeBytes + 1024));
         return std::max(1, std::min({by_regs, by_smem, 4}));
     };
-    per_sm = resident((const void *)k_collocate_tiled, sizeof(SmemColl));
-    const int per_sm_i = resident((const void *)k_integrate_tiled, sizeof(SmemInt));
+    per_sm = std::min(resident(kc[0], sizeof(SmemColl)), resident(kc[1], sizeof(SmemColl)));
+    const int per_sm_i = std::min(resident(ki[0], sizeof(SmemInt)), resident(ki[1], sizeof(SmemInt)));
     M->per_sm = per_sm;
     M->per_sm_i = per_sm_i;
     M->grid_ctas_i = std::max(1, std::min(ntiles, sms * per_sm_i));
     M->grid_ctas = std::max(1, std::min(ntiles, sms * per_sm));
+    M->sms = sms;
     return GPW_SUCCESS;
 }
 
@@ -1396,26 +1733,29 @@ void mixed_free(TaskSet &ts) {
     cudaFree(M->d_items);
     cudaFree(M->d_iimg);
     cudaFree(M->d_queue);
+    cudaFree(M->d_glv);
     delete M;
     ts.mixed = nullptr;
 }
 
-static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which) {
+static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which, bool general) {
     const MixedState &M = *ts.mixed;
+    const int t0 = general ? M.ntiles_ortho : 0;
     MixedArgs a;
     a.blob = M.d_blob;
     a.geoms = ts.d_geom;
     a.levels = ts.plan->d_levels;
-    a.tiles = M.d_tiles;
-    a.start = M.d_start;
+    a.tiles = M.d_tiles + t0;
+    a.start = M.d_start + t0;
     a.items = M.d_items;
     a.iimg = M.d_iimg;
     a.table = ts.d_table;
+    a.glv = M.d_glv;
     a.mom = ts.d_mom;
     a.grids = g;
-    a.queue = M.d_queue + which;
+    a.queue = M.d_queue + which + (general ? 2 : 0);
     a.status = ts.d_status;
-    a.ntiles = M.ntiles;
+    a.ntiles = general ? M.ntiles - M.ntiles_ortho : M.ntiles_ortho;
     return a;
 }
 
@@ -1428,30 +1768,52 @@ cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
     if (!ts.mixed) return cudaErrorNotSupported;
     const MixedState &M = *ts.mixed;
     cudaError_t e = cudaSuccess;
-    if (M.northo > 0 && M.ntiles > 0) {
+    if (M.nbin > 0 && M.ntiles > 0) {
         ts.n_kernels++;
-        k_coef_to_blob<<<(unsigned)std::min<int64_t>((M.northo + 7) / 8, 8192), 256, 0, s>>>(ts.d_coef, M.d_blob,
-                                                                                               M.d_blob_off, M.northo);
-        if ((e = cudaMemsetAsync(M.d_queue, 0, sizeof(int), s)) != cudaSuccess) return e;
-        ProfScope prof(ts, s);
-        k_collocate_tiled<<<M.grid_ctas, NTHR, sizeof(SmemColl), s>>>(make_args(ts, g, 0));
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        k_coef_to_blob<<<(unsigned)std::min<int64_t>((M.nbin + 7) / 8, 8192), 256, 0, s>>>(ts.d_coef, M.d_blob,
+                                                                                             M.d_blob_off, M.nbin);
+        const int nto = M.ntiles_ortho, ntg = M.ntiles - M.ntiles_ortho;
+        if (nto > 0) {
+            if ((e = cudaMemsetAsync(M.d_queue, 0, sizeof(int), s)) != cudaSuccess) return e;
+            ProfScope prof(ts, s);
+            k_collocate_tiled<false><<<std::min(nto, M.sms * M.per_sm), NTHR, sizeof(SmemColl), s>>>(
+                make_args(ts, g, 0, false));
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        if (ntg > 0) {
+            if ((e = cudaMemsetAsync(M.d_queue + 2, 0, sizeof(int), s)) != cudaSuccess) return e;
+            ProfScope prof(ts, s);
+            k_collocate_tiled<true><<<std::min(ntg, M.sms * M.per_sm), NTHR, sizeof(SmemColl), s>>>(
+                make_args(ts, g, 0, true));
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
     }
-    return general_ff(ts, g, false, s);
+    return M.gen_tiled ? cudaSuccess : general_ff(ts, g, false, s);
 }
 
 cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
     if (!ts.mixed) return cudaErrorNotSupported;
     const MixedState &M = *ts.mixed;
     cudaError_t e = cudaSuccess;
-    if (M.northo > 0 && M.ntiles > 0) {
+    if (M.nbin > 0 && M.ntiles > 0) {
         if ((e = cudaMemsetAsync(ts.d_mom, 0, sizeof(double) * ts.coef_len, s)) != cudaSuccess) return e;
-        if ((e = cudaMemsetAsync(M.d_queue + 1, 0, sizeof(int), s)) != cudaSuccess) return e;
-        ProfScope prof(ts, s);
-        k_integrate_tiled<<<M.grid_ctas_i, NTHR, sizeof(SmemInt), s>>>(make_args(ts, g, 1));
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        const int nto = M.ntiles_ortho, ntg = M.ntiles - M.ntiles_ortho;
+        if (nto > 0) {
+            if ((e = cudaMemsetAsync(M.d_queue + 1, 0, sizeof(int), s)) != cudaSuccess) return e;
+            ProfScope prof(ts, s);
+            k_integrate_tiled<false><<<std::min(nto, M.sms * M.per_sm_i), NTHR, sizeof(SmemInt), s>>>(
+                make_args(ts, g, 1, false));
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
+        if (ntg > 0) {
+            if ((e = cudaMemsetAsync(M.d_queue + 3, 0, sizeof(int), s)) != cudaSuccess) return e;
+            ProfScope prof(ts, s);
+            k_integrate_tiled<true><<<std::min(ntg, M.sms * M.per_sm_i), NTHR, sizeof(SmemInt), s>>>(
+                make_args(ts, g, 1, true));
+            if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        }
     }
-    return general_ff(ts, g, true, s);
+    return M.gen_tiled ? cudaSuccess : general_ff(ts, g, true, s);
 }
 
 }  // namespace gpw

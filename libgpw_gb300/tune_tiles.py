@@ -18,7 +18,7 @@ from . import autotune, capi, tasks as T
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--configs", type=int, nargs="+", default=[1, 2, 4, 5])
+    ap.add_argument("--configs", type=int, nargs="+", default=[1, 2, 3, 4, 5])
     ap.add_argument("--npairs", type=int, default=None)
     ap.add_argument("--out", default=None, help="table file (default: the package table)")
     args = ap.parse_args(argv)
@@ -33,7 +33,7 @@ def main(argv=None):
         t0 = time.perf_counter()
         tz, ms = ts.autotune(pab)
         table[key] = {"tile_z": tz, "ms": [[round(float(v), 3) for v in row] for row in ms],
-                      "candidates_tz": [8, 4], "workload": wl.name}
+                      "candidates_tz": [8, 4, 0], "workload": wl.name}
         print(f"config {c} {wl.name}: tile z {tz}  ms {ms.tolist()}  ({time.perf_counter() - t0:.1f} s)", flush=True)
         autotune.save_table(table, args.out)
         ts.close()

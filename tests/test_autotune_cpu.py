@@ -25,4 +25,4 @@ def test_table_round_trip(tmp_path):
 def test_shipped_table_is_valid():
     tab = autotune.load_table(autotune.DEFAULT_TABLE)
     for key, ent in tab.items():
-        assert all(tz in (4, 8) for tz in ent["tile_z"]), key
+        assert all(tz in (0, 4, 8) for tz in ent["tile_z"]), key

@@ -75,28 +75,35 @@ def test_mixed_multigrid(oracle_lib):
         assert rel_l2(g, w) <= TOL
 
 
-def test_mixed_general_cell(oracle_lib):
-    """General-cell pairs of a mixed call run on the float-float general kernel
-    (the reference's row i-ranges, float-float polynomial and exponential)."""
+@pytest.mark.parametrize("tz", [0, 8])
+def test_mixed_general_cell(oracle_lib, tz):
+    """General-cell pairs of a mixed call: tz = 0 runs the float-float general
+    kernel, tz = 8 the tiled tensor-core kernels (cross factor per point)."""
     wl = T.config(3, npairs=40)
     wl.tasks["radius"] = np.minimum(wl.tasks["radius"], 4.0)
-    got = run_collocate(wl, "mixed")[0]
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    ts.set_tiles([tz])
+    assert ts.tiles() == [tz]
+    got = run_collocate(wl, "mixed", ts=ts, plan=plan)[0]
     want = oracle_lib.batch(wl, nthreads=8)[0]
     assert rel_l2(got, want) <= TOL
     V = wl.potentials(seed=6)
-    h = run_integrate(wl, V, "mixed")
+    h = run_integrate(wl, V, "mixed", ts=ts, plan=plan)
     hw = oracle_lib.batch(wl, V=V, nthreads=8)
     assert np.abs(h - hw).max() <= TOL * np.abs(hw).max()
 
 
+@pytest.mark.parametrize("tz", [0, 8])
 @pytest.mark.parametrize("name", [n for n in SET_NAMES if n.startswith("general")])
-def test_mixed_general_sets_vs_fp64(name):
+def test_mixed_general_sets_vs_fp64(name, tz):
     """The general-cell golden sets: mixed against the FP64 path of the same task set."""
     wl, _, V, _ = load_set(name)
     if V is None:
         V = wl.potentials(seed=3)
     plan = capi.Plan(wl.levels)
     ts = capi.TaskSet.from_workload(plan, wl)
+    ts.set_tiles([tz] * len(wl.levels))
     g64 = run_collocate(wl, "fp64", ts=ts, plan=plan)
     gmx = run_collocate(wl, "mixed", ts=ts, plan=plan)
     for a, b in zip(gmx, g64):
@@ -104,6 +111,7 @@ def test_mixed_general_sets_vs_fp64(name):
     h64 = run_integrate(wl, V, "fp64", ts=ts, plan=plan)
     hmx = run_integrate(wl, V, "mixed", ts=ts, plan=plan)
     assert np.abs(hmx - h64).max() <= TOL * np.abs(h64).max()
+
 
 def test_mixed_empty_and_repeat():
     """No pairs: the grid stays zero; a second call accumulates (grid += rho)."""
