@@ -55,6 +55,7 @@ struct TileDesc {
     int level;
     int t[3];  // tile indices
     int lz;    // log2 TZ (TY = MROWS >> lz)
+    int split; // the tile's pairs are divided among several work units: flush with atomics
 };
 
 // tile extents of a tile descriptor
@@ -118,7 +119,7 @@ struct MixedState {
     TileDesc *d_tiles = nullptr;
     uint4 *d_blob = nullptr;       // pair blobs of the orthorhombic tasks (sorted order)
     int64_t *d_blob_off = nullptr; // per task: blob offset in 16-byte chunks
-    int64_t *d_start = nullptr;    // ntiles + 1
+    int64_t *d_start = nullptr;    // per work unit: first item, end
     uint64_t *d_items = nullptr;   // per (tile, pair): blob offset << 16 | chunks
     ItemImg *d_iimg = nullptr;     // per (tile, pair): images
     int *d_queue = nullptr;      // [0]: collocate, [1]: integrate (orthorhombic tiles), [2], [3]: general tiles
@@ -820,7 +821,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
         for (int x = 0; x < TX; x++) acc_hi[x] = acc_lo[x] = 0.0f;
         const int ext_z = min(TZ, lv.ngrid[2] - td.t[2] * TZ), ext_y = min(TY, lv.ngrid[1] - td.t[1] * TY);
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
-        const int64_t it0 = A.start[tile], it1 = A.start[tile + 1];
+        const int64_t it0 = A.start[2 * tile], it1 = A.start[2 * tile + 1];
         uint64_t nxt = 0;
         first_pair(cm, sm.pb, A, it0, it1, nxt, true);
         for (int64_t it = it0; it < it1 && !cm.abort; it++) {
@@ -1016,9 +1017,15 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
             double *grid = A.grids.p[td.level];
             const int64_t row = ((int64_t)(td.t[2] * TZ + z) * lv.ngrid[1] + (td.t[1] * TY + y)) * lv.ngrid[0] +
                                 td.t[0] * TX;
+            if (td.split) {  // other work units add to the same tile
 #pragma unroll
-            for (int x = 0; x < TX; x++)
-                if (x < ext_x) grid[row + x] += (double)acc_hi[x] + (double)acc_lo[x];
+                for (int x = 0; x < TX; x++)
+                    if (x < ext_x) atomicAdd(grid + row + x, (double)acc_hi[x] + (double)acc_lo[x]);
+            } else {
+#pragma unroll
+                for (int x = 0; x < TX; x++)
+                    if (x < ext_x) grid[row + x] += (double)acc_hi[x] + (double)acc_lo[x];
+            }
         }
         __syncthreads();
     }
@@ -1094,7 +1101,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
             }
         }
         bool zero_row[2] = {false, false};  // A rows u, u + 64 hold zeros (warps 2-3)
-        const int64_t it0 = A.start[tile], it1 = A.start[tile + 1];
+        const int64_t it0 = A.start[2 * tile], it1 = A.start[2 * tile + 1];
         uint64_t nxt = 0;
         first_pair(cm, sm.pb, A, it0, it1, nxt, false);
         for (int64_t it = it0; it < it1 && !cm.abort; it++) {
@@ -1371,7 +1378,7 @@ __global__ void k_item_images(const TileDesc *__restrict__ tiles, const int64_t 
         const TileDesc td = tiles[tile];
         const LevelDev &lv = levels[td.level];
         const int ext_x = min(TX, lv.ngrid[0] - td.t[0] * TX);
-        for (int64_t it = start[tile] + threadIdx.x; it < start[tile + 1]; it += blockDim.x) {
+        for (int64_t it = start[2 * tile] + threadIdx.x; it < start[2 * tile + 1]; it += blockDim.x) {
             const TPair &p = *reinterpret_cast<const TPair *>(blob + (items[it] >> 16));
             int img[3][kMaxImages], n[3];
             axis_images(lv, 0, td.t[0], TX, p, img[0], n[0], status);
@@ -1550,19 +1557,38 @@ int mixed_build(TaskSet &ts, std::string &err) {
         }
     };
     each([&](int t, int) { count[t + 1]++; });
-    // order tiles by decreasing work for the persistent queue
-    std::vector<int> order(ntiles);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {  // within each group (ortho, general)
-        const bool ga = a >= nto, gb = b >= nto;
-        if (ga != gb) return !ga;
-        return count[a + 1] > count[b + 1];
-    });
-    std::vector<int> rank(ntiles);
-    for (int i = 0; i < ntiles; i++) rank[order[i]] = i;
+    // items grouped by tile
     std::vector<int64_t> start(ntiles + 1, 0);
-    for (int i = 0; i < ntiles; i++) start[i + 1] = start[i] + count[order[i] + 1];
+    for (int i = 0; i < ntiles; i++) start[i + 1] = start[i] + count[i + 1];
     const int64_t nitems = start[ntiles];
+    // Work units for the persistent queue: a tile with more items than ~1/4 of
+    // an even share per resident CTA is divided into units of consecutive items
+    // (their flushes add with FP64 atomics); units ordered by decreasing work
+    // within each group (orthorhombic, general).
+    int sms_dev = 0;
+    cudaDeviceGetAttribute(&sms_dev, cudaDevAttrMultiProcessorCount, P.device);
+    const int64_t target = std::max<int64_t>(64, (nitems + 16LL * sms_dev - 1) / std::max(1, 16 * sms_dev));
+    struct Unit {
+        int tile;
+        int64_t it0, it1;
+        bool split;
+    };
+    std::vector<Unit> units;
+    for (int t = 0; t < ntiles; t++) {
+        const int64_t n = count[t + 1];
+        if (n == 0) continue;
+        const int64_t nu = (n + target - 1) / target;
+        for (int64_t u = 0; u < nu; u++)
+            units.push_back(Unit{t, start[t] + n * u / nu, start[t] + n * (u + 1) / nu, nu > 1});
+    }
+    std::stable_sort(units.begin(), units.end(), [&](const Unit &a, const Unit &b) {
+        const bool ga = a.tile >= nto, gb = b.tile >= nto;
+        if (ga != gb) return !ga;
+        return a.it1 - a.it0 > b.it1 - b.it0;
+    });
+    const int nunits = (int)units.size();
+    int nuo = 0;
+    while (nuo < nunits && units[nuo].tile < nto) nuo++;
     // blob layout: per task the record, then its coefficients
     std::vector<int64_t> off16((size_t)std::max<int64_t>(nbin, 1), 0);
     std::vector<int> len16((size_t)std::max<int64_t>(nbin, 1), 0);
@@ -1574,10 +1600,17 @@ int mixed_build(TaskSet &ts, std::string &err) {
     }
     std::vector<uint64_t> items((size_t)std::max<int64_t>(nitems, 1));
     std::vector<int64_t> fill(start.begin(), start.end() - 1);
-    each([&](int t, int k) { items[fill[rank[t]]++] = ((uint64_t)off16[k] << 16) | (uint64_t)len16[k]; });
-    std::vector<TileDesc> tiles_sorted(ntiles);
-    for (int i = 0; i < ntiles; i++) tiles_sorted[i] = tiles[order[i]];
-    M->ntiles = ntiles;
+    each([&](int t, int k) { items[fill[t]++] = ((uint64_t)off16[k] << 16) | (uint64_t)len16[k]; });
+    std::vector<TileDesc> tiles_sorted(std::max(nunits, 1));
+    std::vector<int64_t> ubounds(2 * (size_t)std::max(nunits, 1), 0);  // per unit: first item, end
+    for (int u = 0; u < nunits; u++) {
+        tiles_sorted[u] = tiles[units[u].tile];
+        tiles_sorted[u].split = units[u].split ? 1 : 0;
+        ubounds[2 * u] = units[u].it0;
+        ubounds[2 * u + 1] = units[u].it1;
+    }
+    M->ntiles_ortho = nuo;
+    M->ntiles = nunits;
     M->nitems = nitems;
     cudaError_t e = cudaSuccess;
     auto alloc = [&](void **p, size_t bytes) {
@@ -1662,25 +1695,25 @@ int mixed_build(TaskSet &ts, std::string &err) {
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         cudaFree(d_recs);
     }
-    alloc((void **)&M->d_tiles, sizeof(TileDesc) * ntiles);
-    alloc((void **)&M->d_start, sizeof(int64_t) * (ntiles + 1));
+    alloc((void **)&M->d_tiles, sizeof(TileDesc) * tiles_sorted.size());
+    alloc((void **)&M->d_start, sizeof(int64_t) * ubounds.size());
     alloc((void **)&M->d_items, sizeof(uint64_t) * items.size());
     alloc((void **)&M->d_iimg, sizeof(ItemImg) * items.size());
     alloc((void **)&M->d_queue, sizeof(int) * 5);  // [4]: status sink of the set-up kernels
     alloc((void **)&M->d_glv, sizeof(GenLevel) * glv.size());
     if (e == cudaSuccess)
         e = cudaMemcpy(M->d_glv, glv.data(), sizeof(GenLevel) * glv.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && ntiles)
-        e = cudaMemcpy(M->d_tiles, tiles_sorted.data(), sizeof(TileDesc) * ntiles, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && nunits)
+        e = cudaMemcpy(M->d_tiles, tiles_sorted.data(), sizeof(TileDesc) * nunits, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-        e = cudaMemcpy(M->d_start, start.data(), sizeof(int64_t) * (ntiles + 1), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(M->d_start, ubounds.data(), sizeof(int64_t) * ubounds.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nitems)
         e = cudaMemcpy(M->d_items, items.data(), sizeof(uint64_t) * nitems, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && nitems) {
         // image overflows are reported by the tiled kernels when they run (a plain
         // FP64 call on this task set must not see them)
-        k_item_images<<<std::min(ntiles, 8192), 128>>>(M->d_tiles, M->d_start, M->d_items, M->d_blob, P.d_levels,
-                                                       M->d_iimg, ntiles, M->d_queue + 4);
+        k_item_images<<<std::max(1, std::min(nunits, 8192)), 128>>>(M->d_tiles, M->d_start, M->d_items, M->d_blob,
+                                                                    P.d_levels, M->d_iimg, nunits, M->d_queue + 4);
         e = cudaGetLastError();
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
     }
@@ -1717,8 +1750,8 @@ int mixed_build(TaskSet &ts, std::string &err) {
     const int per_sm_i = std::min(resident(ki[0], sizeof(SmemInt)), resident(ki[1], sizeof(SmemInt)));
     M->per_sm = per_sm;
     M->per_sm_i = per_sm_i;
-    M->grid_ctas_i = std::max(1, std::min(ntiles, sms * per_sm_i));
-    M->grid_ctas = std::max(1, std::min(ntiles, sms * per_sm));
+    M->grid_ctas_i = std::max(1, std::min(nunits, sms * per_sm_i));
+    M->grid_ctas = std::max(1, std::min(nunits, sms * per_sm));
     M->sms = sms;
     return GPW_SUCCESS;
 }
@@ -1746,7 +1779,7 @@ static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which, bool
     a.geoms = ts.d_geom;
     a.levels = ts.plan->d_levels;
     a.tiles = M.d_tiles + t0;
-    a.start = M.d_start + t0;
+    a.start = M.d_start + 2 * t0;
     a.items = M.d_items;
     a.iimg = M.d_iimg;
     a.table = ts.d_table;
