@@ -1567,7 +1567,7 @@ int mixed_build(TaskSet &ts, std::string &err) {
     // within each group (orthorhombic, general).
     int sms_dev = 0;
     cudaDeviceGetAttribute(&sms_dev, cudaDevAttrMultiProcessorCount, P.device);
-    const int64_t target = std::max<int64_t>(64, (nitems + 16LL * sms_dev - 1) / std::max(1, 16 * sms_dev));
+    const int64_t target = std::max<int64_t>(64, (nitems + 64LL * sms_dev - 1) / std::max(1, 64 * sms_dev));
     struct Unit {
         int tile;
         int64_t it0, it1;
