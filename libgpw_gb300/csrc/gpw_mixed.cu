@@ -964,46 +964,57 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 // tcgen05.ld is warp-collective: chunk decisions are made per warp
                 if (__any_sync(0xffffffffu, x0 <= x1)) {
                     const float rs = pow2i(max(em - 2 * SLB, -126));
-#pragma unroll
+                    // one chunk of 8 x per iteration (a compact loop body: instruction fetch is
+                    // the kernel's first stall); acc_hi[0..7] always holds the current chunk's
+                    // sums, rotated by 8 after each chunk (four rotations restore the order)
+#pragma unroll 1
                     for (int c = 0; c < TX / 8; c++) {
-                        if (!__any_sync(0xffffffffu, x0 <= x1 && 8 * c <= x1 && 8 * c + 7 >= x0)) continue;
-                        uint32_t r2[8], r3[8], r4[8], r5[8];
-                        const float4 csa = reinterpret_cast<const float4 *>(sm.cs)[2 * c];
-                        const float4 csb = reinterpret_cast<const float4 *>(sm.cs)[2 * c + 1];
-                        const float csv[8] = {csa.x, csa.y, csa.z, csa.w, csb.x, csb.y, csb.z, csb.w};
-                        tc::tmem_ld8(tbase + 8 * c, r2);
-                        tc::tmem_ld8(tbase + 32 + 8 * c, r3);
-                        tc::tmem_ld8(tbase + 64 + 8 * c, r4);
-                        tc::tmem_ld8(tbase + 96 + 8 * c, r5);
-                        tc::tmem_wait_ld32(r2, r3, r4, r5);
+                        if (__any_sync(0xffffffffu, x0 <= x1 && 8 * c <= x1 && 8 * c + 7 >= x0)) {
+                            uint32_t r2[8], r3[8], r4[8], r5[8];
+                            const float4 csa = reinterpret_cast<const float4 *>(sm.cs)[2 * c];
+                            const float4 csb = reinterpret_cast<const float4 *>(sm.cs)[2 * c + 1];
+                            const float csv[8] = {csa.x, csa.y, csa.z, csa.w, csb.x, csb.y, csb.z, csb.w};
+                            tc::tmem_ld8(tbase + 8 * c, r2);
+                            tc::tmem_ld8(tbase + 32 + 8 * c, r3);
+                            tc::tmem_ld8(tbase + 64 + 8 * c, r4);
+                            tc::tmem_ld8(tbase + 96 + 8 * c, r5);
+                            tc::tmem_wait_ld32(r2, r3, r4, r5);
 #pragma unroll
-                        for (int i = 0; i < 8; i++) {
-                            const int x = 8 * c + i;
-                            const bool in = x >= x0 && x <= x1;  // straight-line code: selects, no branches
-                            // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
-                            // lo the exact remainder (fast two-sum), then an exact two-sum into
-                            // acc_hi: acc_lo then only gathers rounding errors and remainders,
-                            // so it stays ~2^-24 below acc_hi however many pairs a point sees
-                            const float d2 = __uint_as_float(r2[i]);
-                            const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
-                                               __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
-                                                         __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
-                            const float scl = __fmul_rn(rs, csv[i]);
-                            const float h0 = __fadd_rn(d2, corr);
-                            float hi = __fmul_rn(h0, scl);
-                            float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
-                            if constexpr (kGeneral) {
-                                if (x > x0) ecur = ff_mul(ecur, eq);  // E(x) on the row's cube points
-                                const ff v = ff_mul(ff{hi, lo}, ecur);
-                                hi = v.hi;
-                                lo = v.lo;
+                            for (int i = 0; i < 8; i++) {
+                                const int x = 8 * c + i;
+                                const bool in = x >= x0 && x <= x1;  // straight-line code: selects, no branches
+                                // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
+                                // lo the exact remainder (fast two-sum), then an exact two-sum into
+                                // acc_hi: acc_lo then only gathers rounding errors and remainders,
+                                // so it stays ~2^-24 below acc_hi however many pairs a point sees
+                                const float d2 = __uint_as_float(r2[i]);
+                                const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
+                                                   __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
+                                                             __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
+                                const float scl = __fmul_rn(rs, csv[i]);
+                                const float h0 = __fadd_rn(d2, corr);
+                                float hi = __fmul_rn(h0, scl);
+                                float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
+                                if constexpr (kGeneral) {
+                                    if (x > x0) ecur = ff_mul(ecur, eq);  // E(x) on the row's cube points
+                                    const ff v = ff_mul(ff{hi, lo}, ecur);
+                                    hi = v.hi;
+                                    lo = v.lo;
+                                }
+                                const float sv = __fadd_rn(acc_hi[i], hi);
+                                const float bb = __fsub_rn(sv, acc_hi[i]);
+                                const float err = __fadd_rn(__fsub_rn(acc_hi[i], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
+                                if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
+                                acc_hi[i] = in ? sv : acc_hi[i];
                             }
-                            const float sv = __fadd_rn(acc_hi[x], hi);
-                            const float bb = __fsub_rn(sv, acc_hi[x]);
-                            const float err = __fadd_rn(__fsub_rn(acc_hi[x], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
-                            if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
-                            acc_hi[x] = in ? sv : acc_hi[x];
                         }
+                        float t8[8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) t8[i] = acc_hi[i];
+#pragma unroll
+                        for (int i = 0; i < TX - 8; i++) acc_hi[i] = acc_hi[i + 8];
+#pragma unroll
+                        for (int i = 0; i < 8; i++) acc_hi[TX - 8 + i] = t8[i];
                     }
                 }
                 tc::fence_before_sync();
@@ -1017,14 +1028,12 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
             double *grid = A.grids.p[td.level];
             const int64_t row = ((int64_t)(td.t[2] * TZ + z) * lv.ngrid[1] + (td.t[1] * TY + y)) * lv.ngrid[0] +
                                 td.t[0] * TX;
-            if (td.split) {  // other work units add to the same tile
 #pragma unroll
-                for (int x = 0; x < TX; x++)
-                    if (x < ext_x) atomicAdd(grid + row + x, (double)acc_hi[x] + (double)acc_lo[x]);
-            } else {
-#pragma unroll
-                for (int x = 0; x < TX; x++)
-                    if (x < ext_x) grid[row + x] += (double)acc_hi[x] + (double)acc_lo[x];
+            for (int x = 0; x < TX; x++) {
+                if (x >= ext_x) continue;
+                const double v = (double)acc_hi[x] + (double)acc_lo[x];
+                if (td.split) atomicAdd(grid + row + x, v);  // other work units add to the same tile
+                else grid[row + x] += v;
             }
         }
         __syncthreads();
