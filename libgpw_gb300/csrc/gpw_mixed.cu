@@ -1077,26 +1077,27 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
             const bool ok = z < ext_z && y < ext_y;
             const int64_t row = ((int64_t)(td.t[2] * TZ + z) * lv.ngrid[1] + (td.t[1] * TY + y)) * lv.ngrid[0] +
                                 td.t[0] * TX;
-            ff v[TX];
-#pragma unroll
-            for (int x = 0; x < TX; x++) v[x] = (ok && x < ext_x) ? ff_from_double(grid[row + x]) : ff{0.0f, 0.0f};
-            if constexpr (kGeneral) {
-#pragma unroll
-                for (int x = 0; x < TX; x++) sm.Vff[x][m] = v[x];
-            }
+            // compact loops (once per tile): the row maximum, then 16-byte chunks of 8 x
             float mx = 0.0f;
-#pragma unroll
-            for (int x = 0; x < TX; x++) mx = fmaxf(mx, fabsf(v[x].hi));
+#pragma unroll 1
+            for (int x = 0; x < TX; x++) {
+                const ff v = (ok && x < ext_x) ? ff_from_double(grid[row + x]) : ff{0.0f, 0.0f};
+                if constexpr (kGeneral) sm.Vff[x][m] = v;
+                mx = fmaxf(mx, fabsf(v.hi));
+            }
             vm = exp_of(mx);
             const float sc = vm == kZeroExp ? 0.0f : pow2i(SLB - vm);
-#pragma unroll
+#pragma unroll 1
             for (int c = 0; c < TX / 8 && !kGeneral; c++) {  // 8 x per 16-byte chunk of the UMMA layout
                 uint32_t w[NSL][4];
 #pragma unroll
                 for (int i = 0; i < 4; i++) {
+                    const int x = 8 * c + 2 * i;
+                    const ff v0 = (ok && x < ext_x) ? ff_from_double(grid[row + x]) : ff{0.0f, 0.0f};
+                    const ff v1 = (ok && x + 1 < ext_x) ? ff_from_double(grid[row + x + 1]) : ff{0.0f, 0.0f};
                     float s0[NSL], s1[NSL];
-                    slice_scaled(v[8 * c + 2 * i], sc, s0);
-                    slice_scaled(v[8 * c + 2 * i + 1], sc, s1);
+                    slice_scaled(v0, sc, s0);
+                    slice_scaled(v1, sc, s1);
 #pragma unroll
                     for (int q = 0; q < NSL; q++) {
                         const __half2 h2 = __floats2half2_rn(s0[q], s1[q]);
@@ -1184,7 +1185,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                     // A operand: V slices of rows u and u + 64 masked to the rows' cube ranges,
                     // 16-byte chunks (8 x of one K half); rows already zero stay untouched
                     const int u = tid - 64;
-#pragma unroll
+#pragma unroll 1
                     for (int rr = 0; rr < 2; rr++) {
                         const int r = u + 64 * rr;
                         const int x0 = sm.rx0[r], x1 = sm.rx1[r];
@@ -1248,7 +1249,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                 phase ^= 1u;
                 if (!ok) break;
                 const bool live = sm.rx0[m] <= sm.rx1[m];
-#pragma unroll
+#pragma unroll 1
                 for (int c = 0; c < KP / 8; c++) {
                     uint32_t ra[8], rb[8], r3[8], r4[8], r5[8];
                     tc::tmem_ld8(tbase + 8 * c, ra);
