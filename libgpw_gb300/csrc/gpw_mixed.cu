@@ -598,18 +598,21 @@ __device__ __forceinline__ uint32_t half_mask(uint32_t b) {
 // The NSL slices of one K = 16 operand row (v[k] for k < kNPow, zero beyond),
 // scaled by sc, as 16-byte chunks of 8 K values in the UMMA layout (planes of
 // plane_halves halves); K groups at or beyond kw are left as they are.
-__device__ __forceinline__ void slice_row16(const ff *v, float sc, int kw, __half *plane0, int plane_halves,
+__device__ __forceinline__ void slice_row16(const ff *vin, float sc, int kw, __half *plane0, int plane_halves,
                                             int row) {
+    // one compact loop body for both K groups: the second group's values are moved down
+    ff v[8];
 #pragma unroll
+    for (int k = 0; k < 8; k++) v[k] = vin[k];
+#pragma unroll 1
     for (int kg = 0; kg < KP / 8; kg++) {
         if (8 * kg >= kw) break;
         uint32_t w[NSL][4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            const int k = 8 * kg + 2 * i;
             float s0[NSL], s1[NSL];
-            slice_scaled(k < kNPow ? v[k < kNPow ? k : 0] : ff{0.0f, 0.0f}, sc, s0);
-            slice_scaled(k + 1 < kNPow ? v[k + 1 < kNPow ? k + 1 : 0] : ff{0.0f, 0.0f}, sc, s1);
+            slice_scaled(v[2 * i], sc, s0);
+            slice_scaled(v[2 * i + 1], sc, s1);
 #pragma unroll
             for (int q = 0; q < NSL; q++) {
                 const __half2 h2 = __floats2half2_rn(s0[q], s1[q]);
@@ -620,6 +623,8 @@ __device__ __forceinline__ void slice_row16(const ff *v, float sc, int kw, __hal
 #pragma unroll
         for (int q = 0; q < NSL; q++)
             reinterpret_cast<uint4 *>(plane0 + q * plane_halves)[o16] = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = 8 + k < kNPow ? vin[8 + k < kNPow ? 8 + k : 0] : ff{0.0f, 0.0f};
     }
 }
 
