@@ -1285,11 +1285,14 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                     }
                 }
                 tc::fence_before_sync();
-                __syncthreads();
-                // stage 2 transposed: T[z][(b,a)] = sum_y S[(z,y)][a] Y[b][y]
-                for (int t = tid; t < TZ * npair; t += NTHR) {
-                    const int zz = t / npair;
-                    int q = t % npair, b = 0;
+                __syncwarp();
+                // stage 2 transposed: T[z][(b,a)] = sum_y S[(z,y)][a] Y[b][y], by the warp whose
+                // rows have this z (a warp barrier after the readout suffices)
+                const int lzw = 5 - sh.ly;  // log2 of the z values per warp
+                const int zbase = (warp * 32) >> sh.ly;
+                for (int t = tid & 31; t < (npair << lzw); t += 32) {
+                    const int zz = zbase + (t & ((1 << lzw) - 1));
+                    int q = t >> lzw, b = 0;
                     while (q >= L - b) { q -= L - b; b++; }
                     const int a = q;
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
