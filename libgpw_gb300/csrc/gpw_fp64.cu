@@ -653,12 +653,6 @@ static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool a
         Chunk c = c0;
         if (extra) c.smem_bytes = c0.smem_ext;
         if (c.count == 0 || (kind >= 0 && c.kind != kind)) continue;
-        const void *fn;
-        if (c.kind == 0)
-            fn = adj ? (const void *)k_ortho_fp64<true> : (const void *)k_ortho_fp64<false>;
-        else
-            fn = adj ? (const void *)k_general_fp64<true> : (const void *)k_general_fp64<false>;
-        (void)fn;
         cudaError_t e;
         ProfScope prof(ts, s);
         if (c.kind == 0) {

@@ -1,8 +1,11 @@
 // Tiled mixed-precision collocate / integrate.
 //
-// Each CTA owns one tile of one grid level (TX x TY x TZ points, x fastest; TX = 32,
-// TY x TZ = 128 rows with TZ = 4 or 8 per level, chosen by the tile autotuner) and
-// walks every pair whose cube touches the tile.  Per pair and tile:
+// Persistent CTAs take work units from an atomic queue.  A unit is one tile of
+// one grid level (TX x TY x TZ points, x fastest; TX = 32, TY x TZ = 128 rows with
+// TZ = 4 or 8 per level, chosen by the tile autotuner) with the pairs whose cube
+// touches it, or a part of that list for the busiest tiles (those units flush
+// with atomics).  The pair records, coefficients and per-tile images are copied
+// one item ahead with cp.async.  Per pair and tile:
 //   1-D tables t^k exp(-zetp t^2) over the tile's three ranges   (float-float)
 //   stage 1  Cxy[z][b][a] = sum_g c[g][b][a] Z[g][z]              (float-float)
 //   stage 2  Cx[(z,y)][a] = sum_b Cxy[z][b][a] Y[b][y]            (float-float)
@@ -17,11 +20,17 @@
 // exact in FP32, so the slice products summed per anti-diagonal s = i+j
 // (D_s = sum over i+j=s of A_i B_j) carry the tensor-core result without FP32
 // accumulation error; the diagonals are recombined in float-float.  The tile sum
-// over pairs is float-float in registers, added to the FP64 grid once per tile.
+// over pairs is float-float (high parts in registers, low parts in shared
+// memory), added to the FP64 grid once per tile.
 //
 // Integrate is the transpose: S[(z,y)][a] = sum_x V[(z,y)][x] X[a][x] by the same
 // slices (V sliced once per tile), then the adjoint stages, and the per-pair
 // moments are added to FP64 scratch with atomics.
+//
+// General (non-orthorhombic) cells use the same kernels instantiated with
+// kGeneral (t_d along the lattice steps, the quadratic row rule, the Gaussian's
+// cross factor per point) when their level has a tile shape; by default they
+// run on the float-float general kernel (gpw_fp64.cu).
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
@@ -783,7 +792,6 @@ __device__ __forceinline__ int item_images(TileCommon &cm, const ItemImg &ii, co
     return nimg;
 }
 
-constexpr uint32_t kWaitLimit = 1u << 24;
 
 // ---------------------------------------------------------------------------
 // kGeneral: tiles of general-cell levels.  The tables, stages and slices are the
@@ -1531,7 +1539,7 @@ int mixed_build(TaskSet &ts, std::string &err) {
         lvl_first[l] = (int)tiles.size();
         for (int a = 0; a < ntz[l]; a++)
             for (int b = 0; b < nty[l]; b++)
-                for (int c = 0; c < ntx[l]; c++) tiles.push_back(TileDesc{l, {c, b, a}, ts.tile_lz[l]});
+                for (int c = 0; c < ntx[l]; c++) tiles.push_back(TileDesc{l, {c, b, a}, ts.tile_lz[l], 0});
     }
     int nto = 0;
     while (nto < (int)tiles.size() && P.lv[tiles[nto].level].ortho) nto++;
