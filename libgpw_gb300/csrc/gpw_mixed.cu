@@ -140,7 +140,8 @@ struct MixedState {
     int grid_ctas = 0;    // collocate
     int grid_ctas_i = 0;  // integrate
     int sms = 0;
-    int per_sm = 0, per_sm_i = 0;
+    int per_sm = 0, per_sm_i = 0, per_sm_ig = 0;  // resident CTAs: collocate, integrate (ortho, general)
+    uint4 *d_vslot = nullptr;  // orthorhombic integrate: per-CTA V slots
 };
 
 
@@ -323,6 +324,7 @@ struct MixedArgs {
     const int *table;
     const GenLevel *glv;  // general levels: FP32 steps, cosines
     double *mom;  // integrate: per-pair moments
+    uint4 *vslot;  // orthorhombic integrate: one slot of kVSlot16 chunks per CTA (the tile's V slices)
     GridPtrs grids;
     int *queue;
     int *status;
@@ -374,7 +376,21 @@ struct alignas(128) SmemColl {
     TileCommon c;
 };
 
-struct alignas(128) SmemInt {
+// The V slices of the tile an orthorhombic integrate CTA works on (the A
+// operand's layout, both K halves, all slices): 32 KB in a per-CTA global slot
+// that stays in L1/L2 while the tile's items are processed.  Kept out of shared
+// memory, they leave room for 4 CTAs per SM.  General cells keep V as
+// float-float in shared memory (the rows are rescaled per image).
+constexpr int kVSlot16 = 2 * NSL * MROWS * KP / 8;
+template <bool kGeneral>
+struct IntVTile {};
+template <>
+struct IntVTile<true> {
+    ff Vff[TX][MROWS];  // general cell: this tile's V (x-major: lanes read consecutive rows)
+};
+
+template <bool kGeneral>
+struct alignas(128) SmemInt : IntVTile<kGeneral> {
     union {
         __half A[2][NSL][MROWS * KP];  // masked V slices, K halves x in [0,16) and [16,32)
         struct {                       // after the MMAs have read A:
@@ -382,21 +398,19 @@ struct alignas(128) SmemInt {
             ff T[kMaxTZ][NPAIR_MAX];   //   stage-2 output T[z][(b,a)]
         } st;
     };
-    union {
-        __half B[2][NSL][KP * KP];        // X' slices, N=16 (alpha) x K=16 per half
-        float xmax[kNPow][TX + 4];        // |X[alpha][x]| for the per-alpha maxima, before B is written
-    };
-    union {
-        __half Vs[2][NSL][MROWS * KP];  // this tile's V slices, unmasked, in the layout of A
-        ff Vff[TX][MROWS];              // general cell: this tile's V (x-major: lanes read consecutive rows)
-    };
+    __half B[2][NSL][KP * KP];  // X' slices, N=16 (alpha) x K=16 per half
     int vmr[MROWS];  // general cell: each row's exponent of V E in the current image
     int gexp[KP];
     signed char rx0[MROWS], rx1[MROWS];  // each row's cube x range in the current image
     PairHdr pb[2];                       // the current pair's record and the one being fetched
     TileCommon c;
 };
-static_assert(sizeof(((SmemInt *)0)->st) <= sizeof(((SmemInt *)0)->A), "S and T fit in A");
+static_assert(sizeof(((SmemInt<false> *)0)->st) <= sizeof(((SmemInt<false> *)0)->A), "S and T fit in A");
+// dynamic shared memory of the orthorhombic integrate CTAs: at least 46 KB, so
+// that no fifth CTA (for which TMEM has no columns left) is placed on an SM
+constexpr size_t kSmemIntOrtho = sizeof(SmemInt<false>) > 46 * 1024 ? sizeof(SmemInt<false>) : 46 * 1024;
+static_assert(kSmemIntOrtho + 1024 <= 228 * 1024 / 4, "4 orthorhombic integrate CTAs per SM");
+static_assert(5 * (kSmemIntOrtho + 1024) > 228 * 1024, "at most 4 orthorhombic integrate CTAs per SM");
 
 // pair index of (b, a), b + a <= lp, rows of constant b
 __device__ __forceinline__ int pair_index(int L, int b, int a) { return b * L - (b * (b - 1)) / 2 + a; }
@@ -1058,9 +1072,10 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
 // V(x) E(x) (E the cross factor of the Gaussian along the row), one row per
 // thread, with its own exponent per row and image.
 template <bool kGeneral>
-__global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
+__global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(MixedArgs A) {
     extern __shared__ __align__(128) unsigned char smraw[];
-    SmemInt &sm = *reinterpret_cast<SmemInt *>(smraw);
+    SmemInt<kGeneral> &sm = *reinterpret_cast<SmemInt<kGeneral> *>(smraw);
+    uint4 *const vslot = kGeneral ? nullptr : A.vslot + (size_t)blockIdx.x * kVSlot16;
     TileCommon &cm = sm.c;
     const int tid = threadIdx.x, warp = tid >> 5;
     const int m = tid;
@@ -1120,7 +1135,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                 const int o16 = (m >> 3) * 16 + (c & 1) * 8 + (m & 7);  // umma_off / 16
 #pragma unroll
                 for (int q = 0; q < NSL; q++)
-                    reinterpret_cast<uint4 *>(sm.Vs[c >> 1][q])[o16] = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
+                    vslot[((c >> 1) * NSL + q) * (MROWS * KP / 8) + o16] = make_uint4(w[q][0], w[q][1], w[q][2], w[q][3]);
             }
         }
         bool zero_row[2] = {false, false};  // A rows u, u + 64 hold zeros (warps 2-3)
@@ -1164,25 +1179,15 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                     // are left as they are (their output columns are not read)
                     ff xv[kNPow];
                     x_column(P, Q, tid, false, xv);
-                    // per-alpha maxima over x through shared memory: lane a < L reduces row a
-#pragma unroll
-                    for (int a = 0; a < kNPow; a++) sm.xmax[a][tid] = fabsf(xv[a].hi);
-                    __syncwarp();
-                    if (tid < L) {
-                        const float4 *row = reinterpret_cast<const float4 *>(sm.xmax[tid]);
-                        float mxb = 0.0f;
-#pragma unroll
-                        for (int j = 0; j < TX / 4; j++) {
-                            const float4 f4 = row[j];
-                            mxb = fmaxf(fmaxf(mxb, fmaxf(f4.x, f4.y)), fmaxf(f4.z, f4.w));
-                        }
-                        sm.gexp[tid] = exp_of(mxb);
-                    }
-                    __syncwarp();
 #pragma unroll
                     for (int a = 0; a < kNPow; a++) {
                         if (a >= L) break;
-                        const int e = sm.gexp[a];
+                        // per-alpha maximum over x: one warp reduction (the bit patterns of
+                        // non-negative floats order as their values)
+                        const float mxb =
+                            __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(fabsf(xv[a].hi))));
+                        const int e = exp_of(mxb);
+                        if (tid == a) sm.gexp[a] = e;
                         const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
                         float sl[NSL];
                         slice_scaled(xv[a], sc, sl);
@@ -1195,7 +1200,7 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                     build_yz(cm, P, Q, lv, td);
                 } else if constexpr (!kGeneral) {
                     bar_sync1(NTHR);
-                    // A operand: V slices of rows u and u + 64 masked to the rows' cube ranges,
+                    // A operand: V slices of rows u and u + 64 (the CTA's slot) masked to the rows' cube ranges,
                     // 16-byte chunks (8 x of one K half); rows already zero stay untouched
                     const int u = tid - 64;
 #pragma unroll 1
@@ -1206,13 +1211,13 @@ __global__ void __launch_bounds__(NTHR, 3) k_integrate_tiled(MixedArgs A) {
                             x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));  // bits x0..x1
                         if (M == 0u && zero_row[rr]) continue;
                         zero_row[rr] = M == 0u;
-                        uint4 val[TX / 8][NSL];  // all loads first: the stores may not pass them
+                        uint4 val[TX / 8][NSL];  // all loads of the row first (from the slot): latencies overlap
 #pragma unroll
                         for (int v = 0; v < TX / 8; v++)
 #pragma unroll
                             for (int q = 0; q < NSL; q++)
-                                val[v][q] = reinterpret_cast<const uint4 *>(
-                                    sm.Vs[v >> 1][q])[(r >> 3) * 16 + (v & 1) * 8 + (r & 7)];
+                                val[v][q] = vslot[((v >> 1) * NSL + q) * (MROWS * KP / 8) + (r >> 3) * 16 +
+                                                  (v & 1) * 8 + (r & 7)];
 #pragma unroll
                         for (int v = 0; v < TX / 8; v++) {
                             const uint32_t mv = M >> (8 * v);
@@ -1754,7 +1759,8 @@ int mixed_build(TaskSet &ts, std::string &err) {
     for (int v = 0; v < 2 && e == cudaSuccess; v++) {
         e = cudaFuncSetAttribute(kc[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemColl));
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(ki[v], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(SmemInt));
+            e = cudaFuncSetAttribute(ki[v], cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(v ? sizeof(SmemInt<true>) : kSmemIntOrtho));
     }
     if (e != cudaSuccess) {
         err = std::string("mixed_build: ") + cudaGetErrorString(e);
@@ -1773,9 +1779,18 @@ int mixed_build(TaskSet &ts, std::string &err) {
         return std::max(1, std::min({by_regs, by_smem, 4}));
     };
     per_sm = std::min(resident(kc[0], sizeof(SmemColl)), resident(kc[1], sizeof(SmemColl)));
-    const int per_sm_i = std::min(resident(ki[0], sizeof(SmemInt)), resident(ki[1], sizeof(SmemInt)));
+    const int per_sm_i = resident(ki[0], kSmemIntOrtho);
     M->per_sm = per_sm;
     M->per_sm_i = per_sm_i;
+    M->per_sm_ig = resident(ki[1], sizeof(SmemInt<true>));
+    // one V slot per resident orthorhombic integrate CTA
+    if (M->ntiles_ortho > 0) {
+        e = cudaMalloc(&M->d_vslot, sizeof(uint4) * kVSlot16 * (size_t)sms * per_sm_i);
+        if (e != cudaSuccess) {
+            err = std::string("mixed_build: ") + cudaGetErrorString(e);
+            return GPW_ERR_CUDA;
+        }
+    }
     M->grid_ctas_i = std::max(1, std::min(nunits, sms * per_sm_i));
     M->grid_ctas = std::max(1, std::min(nunits, sms * per_sm));
     M->sms = sms;
@@ -1793,6 +1808,7 @@ void mixed_free(TaskSet &ts) {
     cudaFree(M->d_iimg);
     cudaFree(M->d_queue);
     cudaFree(M->d_glv);
+    cudaFree(M->d_vslot);
     delete M;
     ts.mixed = nullptr;
 }
@@ -1811,6 +1827,7 @@ static MixedArgs make_args(const TaskSet &ts, const GridPtrs &g, int which, bool
     a.table = ts.d_table;
     a.glv = M.d_glv;
     a.mom = ts.d_mom;
+    a.vslot = M.d_vslot;
     a.grids = g;
     a.queue = M.d_queue + which + (general ? 2 : 0);
     a.status = ts.d_status;
@@ -1860,14 +1877,14 @@ cudaError_t launch_integrate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStr
         if (nto > 0) {
             if ((e = cudaMemsetAsync(M.d_queue + 1, 0, sizeof(int), s)) != cudaSuccess) return e;
             ProfScope prof(ts, s);
-            k_integrate_tiled<false><<<std::min(nto, M.sms * M.per_sm_i), NTHR, sizeof(SmemInt), s>>>(
+            k_integrate_tiled<false><<<std::min(nto, M.sms * M.per_sm_i), NTHR, kSmemIntOrtho, s>>>(
                 make_args(ts, g, 1, false));
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
         if (ntg > 0) {
             if ((e = cudaMemsetAsync(M.d_queue + 3, 0, sizeof(int), s)) != cudaSuccess) return e;
             ProfScope prof(ts, s);
-            k_integrate_tiled<true><<<std::min(ntg, M.sms * M.per_sm_i), NTHR, sizeof(SmemInt), s>>>(
+            k_integrate_tiled<true><<<std::min(ntg, M.sms * M.per_sm_ig), NTHR, sizeof(SmemInt<true>), s>>>(
                 make_args(ts, g, 1, true));
             if ((e = cudaGetLastError()) != cudaSuccess) return e;
         }
