@@ -1018,20 +1018,21 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                                 const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
                                                    __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
                                                              __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
-                                const float scl = __fmul_rn(rs, csv[i]);
+                                float scl = __fmul_rn(rs, csv[i]);
                                 const float h0 = __fadd_rn(d2, corr);
                                 float hi = __fmul_rn(h0, scl);
-                                float lo = __fmul_rn(__fsub_rn(corr, __fsub_rn(h0, d2)), scl);
+                                float rem = __fsub_rn(corr, __fsub_rn(h0, d2));  // lo = rem scl exactly
                                 if constexpr (kGeneral) {
                                     if (x > x0) ecur = ff_mul(ecur, eq);  // E(x) on the row's cube points
-                                    const ff v = ff_mul(ff{hi, lo}, ecur);
+                                    const ff v = ff_mul(ff{hi, __fmul_rn(rem, scl)}, ecur);
                                     hi = v.hi;
-                                    lo = v.lo;
+                                    rem = v.lo;
+                                    scl = 1.0f;
                                 }
                                 const float sv = __fadd_rn(acc_hi[i], hi);
                                 const float bb = __fsub_rn(sv, acc_hi[i]);
                                 const float err = __fadd_rn(__fsub_rn(acc_hi[i], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
-                                if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fadd_rn(err, lo));
+                                if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fmaf_rn(rem, scl, err));
                                 acc_hi[i] = in ? sv : acc_hi[i];
                             }
                         }
