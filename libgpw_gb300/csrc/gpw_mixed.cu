@@ -1270,6 +1270,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                 const bool live = sm.rx0[m] <= sm.rx1[m];
 #pragma unroll 1
                 for (int c = 0; c < KP / 8; c++) {
+                    if (8 * c >= L) break;  // uniform: S columns alpha >= L are not read
                     uint32_t ra[8], rb[8], r3[8], r4[8], r5[8];
                     tc::tmem_ld8(tbase + 8 * c, ra);
                     tc::tmem_ld8(tbase + 16 + 8 * c, rb);
