@@ -111,8 +111,8 @@ class Clocks:
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of this workload at
 # full size: profiles/dram_traffic_pairs1M_l4_256cubed.md
 TRAFFIC = {
-    ("pairs1M_l4_256cubed", 1000000, "k_collocate_tiled"): 19.766249e9 + 0.327932e9,
-    ("pairs1M_l4_256cubed", 1000000, "k_integrate_tiled"): 16.698737e9 + 6.401529e9,
+    ("pairs1M_l4_256cubed", 1000000, "k_collocate_tiled"): 19.678038e9 + 0.326584e9,
+    ("pairs1M_l4_256cubed", 1000000, "k_integrate_tiled"): 20.574986e9 + 8.899182e9,
 }
 
 
@@ -401,7 +401,7 @@ def main():
                 "frac": achieved_tf / peak, "traffic": TRAFFIC.get((wl.name, wl.ntasks, kname)),
                 "peak_source": "bf16 sustained, MEASURED_PEAKS.json (of measured)",
                 "limiter": "FP32/integer instruction issue of the float-float stages, not the tensor pipe "
-                           "(tensor pipe active ~4%, issue slots busy 62% collocate / 44% integrate in the ncu captures)"}
+                           "(tensor pipe active ~4%, issue slots busy 61% collocate / 52% integrate in the ncu captures)"}
     else:
         hbm = peaks.get("hbm_gbs") or 6800.0
         gbytes_alg = 16.0 * points  # FP64 read+write per cube point (no reuse)
