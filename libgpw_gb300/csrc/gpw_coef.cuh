@@ -71,6 +71,10 @@ struct CoefWs {
     }
 };
 
+// al[ax][i][j][k]: the coefficients of (x-a)^i (x-b)^j in powers of (x-p), as the
+// product (u + pa)^i (u + pb)^j with u = x - p, pa = p - a, pb = p - b, expanded by
+// one multiplication by (u + pa) or (u + pb) at a time (no divisions, no power
+// loops): at most (i + j)(i + j + 3)/2 FP64 multiply-adds per (ax, i, j).
 __device__ inline void fill_alpha(CoefWs &w, const PairGeom &g) {
     const int n = 3 * (w.d.A + 1) * (w.d.B + 1);
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
@@ -80,19 +84,13 @@ __device__ inline void fill_alpha(CoefWs &w, const PairGeom &g) {
         const double pa = g.rp[ax] - g.ra[ax];
         const double pb = g.rp[ax] - g.rb[ax];
         double *out = &w.AL(ax, i, j, 0);
-        for (int k = 0; k < w.d.L; k++) out[k] = 0.0;
-        double ci = 1.0;  // C(i, k1)
-        for (int k1 = 0; k1 <= i; k1++) {
-            double pai = 1.0;
-            for (int e = 0; e < i - k1; e++) pai *= pa;
-            double cj = 1.0;
-            for (int k2 = 0; k2 <= j; k2++) {
-                double pbj = 1.0;
-                for (int e = 0; e < j - k2; e++) pbj *= pb;
-                out[k1 + k2] += ci * pai * cj * pbj;
-                cj = cj * (double)(j - k2) / (double)(k2 + 1);
-            }
-            ci = ci * (double)(i - k1) / (double)(k1 + 1);
+        out[0] = 1.0;
+        for (int k = 1; k < w.d.L; k++) out[k] = 0.0;
+        for (int m = 0; m < i + j; m++) {  // degree m so far
+            const double c = m < i ? pa : pb;
+            out[m + 1] = out[m];
+            for (int k = m; k >= 1; k--) out[k] = fma(c, out[k], out[k - 1]);
+            out[0] *= c;
         }
     }
 }
