@@ -24,8 +24,9 @@
 // memory), added to the FP64 grid once per tile.
 //
 // Integrate is the transpose: S[(z,y)][a] = sum_x V[(z,y)][x] X[a][x] by the same
-// slices (V sliced once per tile), then the adjoint stages, and the per-pair
-// moments are added to FP64 scratch with atomics.
+// slices (V sliced once per tile into a per-CTA global slot that stays in L1/L2,
+// copied per pair into the operand with the pair's row masks), then the adjoint
+// stages, and the per-pair moments are added to FP64 scratch with atomics.
 //
 // General (non-orthorhombic) cells use the same kernels instantiated with
 // kGeneral (t_d along the lattice steps, the quadratic row rule, the Gaussian's
