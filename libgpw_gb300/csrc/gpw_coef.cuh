@@ -46,7 +46,9 @@ struct CoefDims {
     GPW_HD int n_al() const { return 3 * (A + 1) * (B + 1) * L; }
     GPW_HD int n_T1() const { return na2 * nb2 * L; }
     GPW_HD int n_T2() const { return (A + 1) * (B + 1) * L * L; }
-    GPW_HD int n_total() const { return n_P() + n_al() + n_T1() + n_T2(); }
+    // P is dead once T1 is formed (forward) and T2 once T1 is formed (adjoint): they share
+    GPW_HD int n_PT2() const { return n_P() > n_T2() ? n_P() : n_T2(); }
+    GPW_HD int n_total() const { return n_al() + n_T1() + n_PT2(); }
 };
 
 // Shared-memory doubles a CTA needs for pairs up to la, lb (local, after tau).
@@ -61,11 +63,12 @@ struct CoefWs {
     double *P, *al, *T1, *T2;
     __device__ void carve(double *base, int A, int B) {
         d.set(A, B);
-        P = base;
-        al = P + d.n_P();
+        al = base;
         T1 = al + d.n_al();
         T2 = T1 + d.n_T1();
+        P = T2;  // shared with T2 (see n_PT2)
     }
+    __device__ double *end() const { return T2 + d.n_PT2(); }
     __device__ double &AL(int ax, int i, int j, int k) {
         return al[((ax * (d.A + 1) + i) * (d.B + 1) + j) * d.L + k];
     }

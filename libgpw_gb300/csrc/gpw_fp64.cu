@@ -63,7 +63,7 @@ __global__ void k_prep(const PairGeom *__restrict__ geoms, const LevelDev *__res
         forward_coef(w, g, coef + g.coef_off);
         return;
     }
-    double *c = w.T2 + w.d.n_T2();  // packed c, before the lattice transform
+    double *c = w.end();  // packed c, before the lattice transform
     forward_coef(w, g, c);
     __syncthreads();
     // q[k][j][i] = sum over same-degree (lz,ly,lx) of T * c; T in lp = kMaxLp packing
@@ -116,7 +116,7 @@ __global__ void k_backtransform(const PairGeom *__restrict__ geoms, const LevelD
     fill_alpha(w, g);
     const int nc = ncoef(g.lp);
     const double *W = mom + g.coef_off;
-    double *Wc = w.T2 + w.d.n_T2();
+    double *Wc = w.end();
     if (!g.ortho) {
         // Wc[lz][ly][lx] = sum over same-degree (k,j,i) of T[(k,j,i)][(lz,ly,lx)] * Wq[k][j][i]
         const LevelDev &lv = levels[g.level];
