@@ -759,7 +759,7 @@ __device__ __forceinline__ void tc_teardown(TileCommon &c, uint32_t ncols, uint3
     if (threadIdx.x < 32) tc::tmem_dealloc(c.tmem, ncols);
 }
 
-// waits for the MMAs of this round; false (and abort flagged) on timeout
+// waits for the MMAs of the current item; false (and abort flagged) on timeout
 __device__ __forceinline__ bool tc_wait(TileCommon &c, uint32_t phase, int *status) {
     if (!tc::mbar_wait_bounded(&c.mbar, phase, 1u << 24)) {
         atomicOr(status, kStatTimeout);
