@@ -26,3 +26,14 @@ def test_shipped_table_is_valid():
     tab = autotune.load_table(autotune.DEFAULT_TABLE)
     for key, ent in tab.items():
         assert all(tz in (0, 4, 8) for tz in ent["tile_z"]), key
+
+
+def test_shipped_table_covers_benchmark_workloads():
+    """The table shipped with the package applies to the five benchmark
+    workloads (a change of the signature would silently drop the tuned shapes)."""
+    tab = autotune.load_table(autotune.DEFAULT_TABLE)
+    for c in (1, 2, 3, 4, 5):
+        wl = T.config(c)
+        key = autotune.signature(wl.levels, wl.tasks)
+        assert key in tab, (c, key)
+        assert len(tab[key]["tile_z"]) == len(wl.levels)
