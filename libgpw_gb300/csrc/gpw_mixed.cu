@@ -15,11 +15,15 @@
 //
 // Stage 3 operands are split into NSL fixed-point fp16 slices of SLB bits: each
 // row of Cx is scaled by a power of two so its largest entry is < 2^SLB, each
-// column of X likewise, and the slices are integers in [-2^SLB, 2^SLB].  Every
-// product of two slices (<= 2^20) and every sum of 16 of them (<= 2^24) is then
-// exact in FP32, so the slice products summed per anti-diagonal s = i+j
-// (D_s = sum over i+j=s of A_i B_j) carry the tensor-core result without FP32
-// accumulation error; the diagonals are recombined in float-float.  The tile sum
+// column of X likewise, and the slices are integers (the first in [-2^SLB,
+// 2^SLB], the others in [-2^(SLB-1), 2^(SLB-1)]).  They carry the float-float
+// operand to ~2^-35 of its row's scale (its low part enters through one float32
+// remainder).  Every slice product is an integer of at most 2^20, so the
+// anti-diagonal sums D_s = sum over i+j=s of A_i B_j are exact in FP32 for the
+// leading two (16 and 32 products, at most 2^24); the next two (3 and 4 MMAs
+// into one accumulator) can pass 2^24 only in the worst case, where their
+// rounding stays below 2^-40 of the scales.  The diagonals are recombined in
+// float-float.  The tile sum
 // over pairs is float-float (high parts in registers, low parts in shared
 // memory), added to the FP64 grid once per tile.
 //
@@ -302,16 +306,6 @@ __device__ __forceinline__ void slice_scaled(ff v, float scale, float *sl) {
         sl[i] = rintf(r);
         r = __fsub_rn(r, sl[i]);
     }
-}
-
-// Combine the diagonals D_2..D_5 of one product (weights 1, 2^-10, 2^-20, 2^-30)
-// into float-float and scale by 2^E.
-__device__ __forceinline__ ff combine(float d2, float d3, float d4, float d5, int E) {
-    ff s = two_sum(d2, __fmul_rn(d3, 0.0009765625f));
-    s.lo = __fmaf_rn(d4, 9.5367431640625e-07f, __fmaf_rn(d5, 9.313225746154785e-10f, s.lo));
-    if (E < -126) return {0.0f, 0.0f};  // below 2^-102 of unit scale: dropped
-    const float sc = __int_as_float((127 + E) << 23);
-    return {__fmul_rn(s.hi, sc), __fmul_rn(s.lo, sc)};
 }
 
 struct MixedArgs {
