@@ -22,7 +22,9 @@
 // anti-diagonal sums D_s = sum over i+j=s of A_i B_j are exact in FP32 for the
 // leading two (16 and 32 products, at most 2^24); the next two (3 and 4 MMAs
 // into one accumulator) can pass 2^24 only in the worst case, where their
-// rounding stays below 2^-40 of the scales.  The diagonals are recombined in
+// rounding stays below 2^-40 of the scales.  (Integrate contracts 32 x: D2 is
+// kept as two K halves of 16 products; its D3 sums 64 and can round in the worst
+// case, by less than 2^-35 of the scales.)  The diagonals are recombined in
 // float-float.  The tile sum
 // over pairs is float-float (high parts in registers, low parts in shared
 // memory), added to the FP64 grid once per tile.
