@@ -185,6 +185,18 @@ def cpu_baseline(wl, seconds: float, seed: int = 0) -> dict:
                       f"{threads} threads with private grids, {elapsed:.1f} s"}
 
 
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """The maximum over the ranks of a per-rank time (the rank itself on one rank)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def reference_arm(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -317,12 +329,7 @@ def main():
     n_kernels += n_kernels_i
     kern_ms = (coll_ms + int_ms) * args.steps
     kern_launches = (coll_launches + int_launches) * args.steps
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, world, dev)
     value = world * wl.ntasks / (ms * 1e-3)
 
     # end to end through the host-buffer C ABI calls (pinned host memory, copies inside the timed region),
@@ -344,7 +351,7 @@ def main():
                 ts.integrate_host(V_h, hab_h, prec)
             torch.cuda.synchronize()
             barrier()
-            e2e_s = (time.perf_counter() - t0) / ne
+            e2e_s = max_over_ranks((time.perf_counter() - t0) / ne, world, dev)
         gbytes = sum(g.nbytes for g in grids_h)
         e2e = {"value": world * wl.ntasks / e2e_s, "unit": "pairs/s",
                "h2d_bytes_per_step": int(pab_h.nbytes + gbytes + sum(v.nbytes for v in V_h) + hab_h.nbytes),
