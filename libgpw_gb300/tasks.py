@@ -1,6 +1,6 @@
 """Task and grid descriptions on the host: numpy mirrors of the C structs in
-include/gpw.h, the seeded synthetic workloads, and a reader for the
-reference's "Grid collocate task v1" text format.
+include/gpw.h, the seeded synthetic workloads, and a reader and a writer for
+the reference's "Grid collocate task v1" text format.
 
 Reference anchors (mtaillefumier/libgpw):
   * per-call arguments of grid_collocate_pgf_product_rspace -> gpw_task / gpw_grid_desc
@@ -9,7 +9,8 @@ Reference anchors (mtaillefumier/libgpw):
     reader src/lib/grid_base_ref_replay.cc:18-273.  This reader reads the whole
     file, keeps the cube of general-cell tasks absent instead of dereferencing it,
     and reports which grid values the file pins (the writer only visits the x=0
-    plane, grid_base_ref_c.cc:1160,1171).
+    plane, grid_base_ref_c.cc:1160,1171).  write_task_file writes the same lines
+    in the same order but pins every nonzero grid value.
 """
 from __future__ import annotations
 
@@ -273,3 +274,48 @@ def read_task_file(path: str) -> dict:
         out["lb_cube"] = np.zeros(3, dtype=np.int32)
         out["ub_cube"] = np.zeros(3, dtype=np.int32)
     return out
+
+
+_TASK_INT_KEYS = ("compute_tau", "use_ortho", "la_max", "la_min", "lb_max", "lb_min")
+
+
+def write_task_file(path: str, task: dict, grid=None) -> int:
+    """Writes a "#Grid collocate task v1" file: the lines of the reference's dump
+    (grid_base_ref_c.cc:1105-1179, same keys and order), doubles with 17
+    significant digits (exact round trip), and every nonzero value of `grid`
+    (the task's own contribution, shape (ngrid[2], ngrid[1], ngrid[0])) as
+    "grid z y x value" - all planes, where the reference's loop visits x = 0 only.
+    `task` holds the fields read_task_file returns.  Returns the number of grid
+    lines written."""
+
+    def f(x):
+        return "%.16e" % float(x)
+
+    def v3(key, conv):
+        return f"{key} " + " ".join(conv(x) for x in np.asarray(task[key]).reshape(3))
+
+    lines = ["#Grid collocate task v1"]
+    lines += [f"{k} {int(task[k])}" for k in _TASK_INT_KEYS]
+    lines += [f"{k} {f(task[k])}" for k in ("zeta", "zetb", "rscale")]
+    dh, dhi = np.asarray(task["dh"]).reshape(3, 3), np.asarray(task["dh_inv"]).reshape(3, 3)
+    lines += [f"dh {i} " + " ".join(f(x) for x in dh[i]) for i in range(3)]
+    lines += [f"dh_inv {i} " + " ".join(f(x) for x in dhi[i]) for i in range(3)]
+    lines += [v3("ra", f), v3("rab", f)]
+    lines += [v3(k, lambda x: str(int(x))) for k in ("npts", "ngrid", "lb_grid", "periodic")]
+    lines += [f"lmax {int(task['lmax'])}", f"radius {f(task['radius'])}"]
+    if int(task["use_ortho"]):
+        lines += [v3(k, lambda x: str(int(x))) for k in ("lb_cube", "ub_cube")]
+    sb = np.asarray(task["sphere_bounds"], dtype=np.int64).reshape(-1)
+    lines += [f"nspheres {int(task['nspheres'])}", f"nspheres_nonzero {int(np.count_nonzero(sb))}"]
+    lines += [f"sphere_bounds {i} {int(v)}" for i, v in enumerate(sb) if v != 0]
+    lines += [f"{k} {int(task[k])}" for k in ("maxco", "o1", "o2")]
+    pab = np.asarray(task["pab"], dtype=np.float64)
+    m = int(task["maxco"])
+    lines += [f"pab {i} {j} {f(pab[i, j])}" for i in range(m) for j in range(m)]
+    nz = np.argwhere(grid != 0.0) if grid is not None else np.zeros((0, 3), dtype=np.int64)
+    lines.append(f"ngrid_nonzero {len(nz)}")
+    lines += [f"grid {z} {y} {x} {f(grid[z, y, x])}" for z, y, x in nz]
+    lines.append("#THE_END")
+    with open(path, "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    return len(nz)

@@ -4,6 +4,7 @@
 // caller arrays in the reference's mdarray (no copies) and calls it unchanged.
 #include <vector>
 #include "grid_base_ref_c.h"
+#include "grid_base_ref_replay.h"
 #include "rt_graph.hpp"
 
 rt_graph::Timer timer;  // the reference expects the caller to define it (grid_base_ref_miniapp.cc:13)
@@ -33,3 +34,11 @@ extern "C" int gpwref_collocate(
                                       o2, pab, grid);
     return 0;
 }
+
+// The reference's own task-file replay (grid_collocate_replay,
+// src/lib/grid_base_ref_replay.cc:18-274): parses a "Grid collocate task v1"
+// file with the reference's reader, collocates it `cycles` times and returns
+// the largest difference to the grid values the file pins.  A malformed file
+// fails the reader's asserts (the process aborts), so callers run it in a
+// child process.
+extern "C" double gpwref_replay(const char *path, int cycles) { return grid_collocate_replay(path, cycles); }

@@ -98,3 +98,62 @@ def test_reference_direct(oracle_lib):
         oracle_lib.collocate(d, a, use_ref=True)
         oracle_lib.collocate(d, b)
         assert rel_l2(b, a) <= 1e-13
+
+
+@pytest.mark.parametrize("name", TASK_NAMES)
+def test_task_file_writer_round_trip(oracle_lib, name, tmp_path):
+    """write_task_file writes the reference's task lines with every nonzero grid
+    value (the reference's dump loop visits x = 0 only): read back, the fields
+    are identical, the file pins the reference's whole grid, and the oracle
+    reproduces it from the file alone."""
+    d = load_task(name)
+    path = str(tmp_path / (name + ".task"))
+    n = T.write_task_file(path, d, d["grid_ref"])
+    assert n == int(np.count_nonzero(d["grid_ref"])) > 0
+    r = T.read_task_file(path)
+    for k in ("compute_tau", "use_ortho", "la_max", "la_min", "lb_max", "lb_min", "lmax", "nspheres",
+              "maxco", "o1", "o2", "zeta", "zetb", "rscale", "radius"):
+        assert r[k] == d[k], k
+    for k in ("dh", "dh_inv", "ra", "rab", "npts", "ngrid", "lb_grid", "periodic", "sphere_bounds", "pab"):
+        assert np.array_equal(np.asarray(r[k]), np.asarray(d[k])), k
+    if d["use_ortho"]:
+        assert np.array_equal(r["lb_cube"], d["lb_cube"]) and np.array_equal(r["ub_cube"], d["ub_cube"])
+    pinned = np.zeros_like(d["grid_ref"])
+    gv = r["grid_values"]
+    pinned[gv[:, 0].astype(int), gv[:, 1].astype(int), gv[:, 2].astype(int)] = gv[:, 3]
+    assert np.array_equal(pinned, d["grid_ref"])
+    grid = np.zeros_like(d["grid_ref"])
+    assert oracle_lib.collocate(r, grid) == 0
+    assert rel_l2(grid, d["grid_ref"]) <= (1e-11 if not d["use_ortho"] else 1e-13)
+
+
+@pytest.mark.parametrize("name", TASK_NAMES)
+def test_task_file_writer_read_by_reference(oracle_lib, name, tmp_path):
+    """Files from write_task_file pass the reference's own reader and replay
+    (grid_collocate_replay, grid_base_ref_replay.cc:18-274, built from the
+    reference sources into oracle/_ref): it parses every line with its asserts,
+    recollocates the task and finds the pinned values it compares equal.  Run in
+    a child process, since a reader assert aborts."""
+    import os
+    import subprocess
+    import sys
+
+    from oracle import oracle as O
+
+    if not O.ref_available():
+        pytest.skip("the reference library is built only where the reference sources are")
+    d = load_task(name)
+    if not d["use_ortho"]:
+        # the reference's replay prints ub_cube[0] of a general-cell task, whose
+        # cube it has set to NULL (grid_base_ref_replay.cc:226): it crashes on
+        # the reference's own general-cell files as well
+        pytest.skip("the reference's replay dereferences the absent cube of general-cell tasks")
+    path = str(tmp_path / (name + ".task"))
+    T.write_task_file(path, d, d["grid_ref"])
+    lib = os.path.join(os.path.dirname(O.__file__), "_ref", "libgpwref.so")
+    code = ("import ctypes, sys; L = ctypes.CDLL(sys.argv[1]); L.gpwref_replay.restype = ctypes.c_double; "
+            "print('MAXDIFF', L.gpwref_replay(sys.argv[2].encode(), 1))")
+    r = subprocess.run([sys.executable, "-c", code, lib, path], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    diff = float([ln for ln in r.stdout.splitlines() if ln.startswith("MAXDIFF")][-1].split()[1])
+    assert diff <= 1e-12 * max(float(np.abs(d["grid_ref"]).max()), 1e-300)
