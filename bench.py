@@ -107,9 +107,10 @@ class Clocks:
 
 
 # ----------------------------------------------------------------------------
-# DRAM bytes (read + write) of one launch of the dominant kernel, from a one-pass
-# ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of this workload at
-# full size: profiles/dram_traffic_pairs1M_l4_256cubed.md
+# DRAM bytes (read + write) of one launch of each tiled kernel on the 1M-pair
+# workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
+# the build these constants were last measured with (the committed profile summary
+# gives the command and the date); None where not captured for the current build.
 TRAFFIC = {
     ("pairs1M_l4_256cubed", 1000000, "k_collocate_tiled"): 19.678038e9 + 0.326584e9,
     ("pairs1M_l4_256cubed", 1000000, "k_integrate_tiled"): 20.574986e9 + 8.899182e9,
@@ -183,6 +184,28 @@ def cpu_baseline(wl, seconds: float, seed: int = 0) -> dict:
     return {"value": len(idx) / elapsed, "unit": "pairs/s", "cores": threads, "kind": kind,
             "sample": f"{len(idx)} random pairs of the {wl.ntasks}-pair workload, collocate+integrate FP64, "
                       f"{threads} threads with private grids, {elapsed:.1f} s"}
+
+
+def fp64_gemm_rate(dev) -> float:
+    """FP64 GEMM rate of this GPU (cuBLAS through torch.matmul, 4096^3, best of
+    5 after one warm-up), TFLOP/s: the rate an FP64 implementation of the
+    contraction could reach at best."""
+    import torch
+
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    c = a @ b
+    best = float("inf")
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
 def max_over_ranks(x: float, world: int, device=None) -> float:
@@ -314,7 +337,7 @@ def main():
         torch.cuda.synchronize()
     barrier()
     ts.check()
-    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    ms = float(np.median([s.elapsed_time(e) for s, e in zip(starts, ends)]))
     # per-kernel device time of the same step, measured on one direct step
     ts.stats()
     ts.profile(True)
@@ -385,6 +408,7 @@ def main():
                "fp64_path": {"value": wl.ntasks / (fp64_ms * 1e-3), "unit": "pairs/s", "ms_per_step": fp64_ms,
                              "timing": "one collocate+integrate of the plain FP64 kernels, CUDA events"}}
         del g1, g2, h1, h2
+        err["fp64_gemm_tflops"] = fp64_gemm_rate(dev)
 
     if rank != 0:
         return
@@ -394,9 +418,9 @@ def main():
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
-    # dominant kernel: the slower of the two contraction kernels (integrate on the
-    # 1M-pair workload); its algorithmic flops (the collocate count, integrate is
-    # symmetric) over its average launch time on the launching stream
+    # dominant kernel: the slower of the two contraction kernels; its algorithmic
+    # flops (the collocate count, integrate is symmetric) over its average launch
+    # time on the launching stream
     dom, dom_ms, dom_n = ("integrate", int_ms, int_launches) if int_ms >= coll_ms else ("collocate", coll_ms, coll_launches)
     per_launch_flops = flops / max(dom_n, 1)
     avg_launch_ms = dom_ms / max(dom_n, 1)
@@ -421,6 +445,18 @@ def main():
     roof["integrate_ms_per_launch"] = int_ms / max(int_launches, 1)
     roof["kernel_launches_per_step"] = kern_launches / args.steps
     roof["algorithmic_tflop_per_step"] = 2 * flops / 1e12
+    # speed-up over the plain FP64 GPU path, and over the time an FP64 code would
+    # need at this GPU's FP64 GEMM rate for the same algorithmic flops
+    vs_fp64 = None
+    if err.get("fp64_path"):
+        bound_ms = 2 * flops / (err["fp64_gemm_tflops"] * 1e12) * 1e3
+        vs_fp64 = {"fp64_gpu_path": err["fp64_path"]["ms_per_step"] / ms,
+                   "fp64_path_tflops": 2 * flops / (err["fp64_path"]["ms_per_step"] * 1e-3) / 1e12,
+                   "fp64_path_frac_of_fp64_gemm": 2 * flops / (err["fp64_path"]["ms_per_step"] * 1e-3) / 1e12
+                   / err["fp64_gemm_tflops"],
+                   "fp64_gemm_rate_bound_ms": bound_ms, "fp64_gemm_rate_bound": bound_ms / ms,
+                   "note": "ratios of step times: plain FP64 GPU path / this step, and the algorithmic "
+                           "flops at the measured FP64 GEMM rate / this step"}
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         cpu = cpu_baseline(wl, args.cpu_seconds)
@@ -438,7 +474,8 @@ def main():
                    "launch": "CUDA graph replay of the step" if graph is not None else "direct launches",
                    "plan_seconds": plan_s, "tile_z": tiles, "tile_source": tile_src, "tune_seconds": tune_s},
         "gpu_launches": int(n_kernels * args.steps),
-        "roofline": roof, "error": err, "clocks": clk.summary(), "cpu_baseline": cpu, "e2e": e2e,
+        "roofline": roof, "error": err, "vs_fp64": vs_fp64, "clocks": clk.summary(), "cpu_baseline": cpu,
+        "e2e": e2e,
         "algorithmic_cube_points": points,
     }
     print(json.dumps(line))

@@ -224,7 +224,9 @@ int gpw_selftest_tensorcore(int64_t *mismatches);
  * each device (make that first call with the device current, and before any
  * stream capture begins).  All calls
  * share it: calls that overlap on the GPU (different streams or threads
- * without ordering) race.  Waits for `stream` before returning.
+ * without ordering) race.  Waits for `stream` before returning and reports
+ * the kernels' error flags as gpw_taskset_check does (GPW_ERR_OUT_OF_WINDOW
+ * when a cube left a non-periodic window).
  * Larger batches: gpw_taskset_create / gpw_collocate.
  */
 #define GPW_NOALLOC_MAX_TASKS 64

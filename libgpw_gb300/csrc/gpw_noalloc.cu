@@ -131,10 +131,26 @@ extern "C" int gpw_collocate_noalloc(const gpw_grid_desc *level, const gpw_task 
     if (e == cudaSuccess)
         e = launch_pairs_fp64(d_geom, d_level, nullptr, d_coef, d_status, ntasks, compute_tau ? 1 : 0, max_A, max_B,
                               smem_coll, d_pab, d_grid, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host copies above read stack memory
+    // the kernels' error bits, read into a stack variable (a copy, no allocation)
+    int flags = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&flags, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // the host copies above read and write stack memory
     if (e != cudaSuccess) {
         set_last_error(std::string("gpw_collocate_noalloc: ") + cudaGetErrorString(e));
         return GPW_ERR_CUDA;
+    }
+    // the same meaning as in gpw_taskset_check
+    if (flags & kStatOutOfWindow) {
+        set_last_error("gpw_collocate_noalloc: a cube left the local grid window; its points outside were skipped");
+        return GPW_ERR_OUT_OF_WINDOW;
+    }
+    if (flags & kStatTimeout) {
+        set_last_error("gpw_collocate_noalloc: a bounded device wait gave up");
+        return GPW_ERR_TIMEOUT;
+    }
+    if (flags) {
+        set_last_error("gpw_collocate_noalloc: device status " + std::to_string(flags));
+        return GPW_ERR_INVALID_ARG;
     }
     return GPW_SUCCESS;
 }

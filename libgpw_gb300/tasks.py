@@ -305,7 +305,8 @@ def write_task_file(path: str, task: dict, grid=None) -> int:
     lines += [f"lmax {int(task['lmax'])}", f"radius {f(task['radius'])}"]
     if int(task["use_ortho"]):
         lines += [v3(k, lambda x: str(int(x))) for k in ("lb_cube", "ub_cube")]
-    sb = np.asarray(task["sphere_bounds"], dtype=np.int64).reshape(-1)
+    # the first nspheres entries, as the reference's dump loop (i < nspheres)
+    sb = np.asarray(task["sphere_bounds"], dtype=np.int64).reshape(-1)[: int(task["nspheres"])]
     lines += [f"nspheres {int(task['nspheres'])}", f"nspheres_nonzero {int(np.count_nonzero(sb))}"]
     lines += [f"sphere_bounds {i} {int(v)}" for i, v in enumerate(sb) if v != 0]
     lines += [f"{k} {int(task[k])}" for k in ("maxco", "o1", "o2")]

@@ -28,10 +28,13 @@ _ARGS = [C.c_int] * 6 + [C.c_double] * 3 + [_dp, _dp, _dp, _dp, _ip, _ip, _ip, _
                                             C.c_int, _dp, _dp]
 
 
-def build(quiet: bool = True) -> None:
-    """Compiles liboracle.so (and _ref when the reference tree is present)."""
-    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True,
-                   stdout=subprocess.DEVNULL if quiet else None)
+def build(quiet: bool = True, ref_src: str | None = None) -> None:
+    """Compiles liboracle.so, and _ref/libgpwref.so from the reference's src/lib
+    directory when one is given (ref_src, or the GPW_REFERENCE_SRC environment
+    variable) and holds the reference sources."""
+    ref_src = ref_src or os.environ.get("GPW_REFERENCE_SRC", "")
+    cmd = ["make", "-s", "-C", HERE, "all"] + ([f"REF={ref_src}"] if ref_src else [])
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL if quiet else None)
 
 
 def lib():

@@ -4,7 +4,7 @@ Run in a tree where the reference sources exist (it reads the reference's task
 fixtures and calls the reference's own grid_collocate_pgf_product_rspace,
 compiled by oracle/ref/Makefile):
 
-    python tests/golden/make_golden.py [--ref-root /root/reference]
+    python tests/golden/make_golden.py --ref-root <reference checkout>
 
 Outputs (tests/golden/):
   reference_tasks.npz  the four "Grid collocate task v1" files of the reference
@@ -137,9 +137,9 @@ def synthetic_sets():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-root", default="/root/reference")
+    ap.add_argument("--ref-root", required=True, help="root of the reference checkout (holds src/lib)")
     args = ap.parse_args()
-    O.build()
+    O.build(ref_src=os.path.join(args.ref_root, "src", "lib"))
     if not O.ref_available():
         sys.exit("reference library not built (reference sources absent?)")
     np.savez_compressed(os.path.join(HERE, "reference_tasks.npz"), **task_files(args.ref_root))
