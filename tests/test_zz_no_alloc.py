@@ -52,7 +52,7 @@ def test_noalloc_reports_out_of_window():
     pab = torch.from_numpy(wl.pab).to(dev)
     grid = torch.zeros(T.grid_shape(wl.levels[0]), dtype=torch.float64, device=dev)
     assert _call(level, tasks, 0, pab, grid) == 3  # GPW_ERR_OUT_OF_WINDOW
-    assert "window" in capi.last_error()
+    assert "local grid" in capi.last_error()
     assert not torch.any(grid)
 
 
