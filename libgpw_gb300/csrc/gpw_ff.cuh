@@ -67,6 +67,20 @@ __device__ __forceinline__ ff ff_fma(ff a, ff b, ff c) {
     return fast_two_sum(s.hi, t);
 }
 
+// s += a*b with the sum kept unnormalised: s.hi takes the rounded sum of the
+// leading products (exact error by two-sum), s.lo gathers the errors and the
+// cross terms.  |s.lo| stays a few ulps of s.hi over short sums; normalise with
+// ff_add / fast_two_sum before the value is used elsewhere.
+__device__ __forceinline__ void ff_acc_lazy(ff &s, ff a, ff b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const ff t = two_sum(s.hi, p);
+    s.hi = t.hi;
+    s.lo = __fadd_rn(s.lo, __fadd_rn(t.lo, e));
+}
+
 // 2^(j/32), j = 0..31, as float-float (hi = the float nearest, lo = the rest)
 __constant__ float2 c_exp2_32[32] = {
     {1.0f, 0.0f},

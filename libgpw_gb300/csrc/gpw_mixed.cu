@@ -370,8 +370,12 @@ struct alignas(128) SmemColl {
     float acc_lo[MROWS][TX + 1];  // low parts of the tile sums (row m belongs to thread m; padded rows)
     float bin[kNPow][kNPow];    // binomials C(a', a) of the re-expansion
     alignas(16) float cs[TX];   // 2^fx per column (0 for an empty column)
+    unsigned char qb[kNPow][NPAIR_MAX + 2];  // qb[L-1][pair_index(L, b, a)] = b
+    int zs[kNPow + 1];          // zs[g]: packed index of (g, 0, 0) for the current pair's lp
     TileCommon c;
 };
+
+static_assert(4 * (sizeof(SmemColl) + 1024) <= 228 * 1024, "4 collocate CTAs per SM");
 
 // The V slices of the tile an orthorhombic integrate CTA works on (the A
 // operand's layout, both K halves, all slices): 32 KB in a per-CTA global slot
@@ -399,6 +403,8 @@ struct alignas(128) SmemInt : IntVTile<kGeneral> {
     int vmr[MROWS];  // general cell: each row's exponent of V E in the current image
     int gexp[KP];
     signed char rx0[MROWS], rx1[MROWS];  // each row's cube x range in the current image
+    unsigned char qb[kNPow][NPAIR_MAX + 2];  // qb[L-1][pair_index(L, b, a)] = b
+    int zs[kNPow + 1];                       // zs[g]: packed index of (g, 0, 0) for the current pair's lp
     PairHdr pb[2];                       // the current pair's record and the one being fetched
     TileCommon c;
 };
@@ -583,23 +589,19 @@ __constant__ float c_binom[kNPow][kNPow] = {
     {1, 10, 45, 120, 210, 252, 210, 120, 45, 10, 1}};
 
 // One item (g, b, a) per thread of [t0, t0 + nt): Horner in tc over a' = amax .. a
-// with the binomials from shared memory (bin[a'][a] = C(a', a)).
-__device__ void recentre_x(const PairBuf &pb, ff tc, ff *out, const float (*bin)[kNPow], int t0, int nt) {
+// with the binomials from shared memory (bin[a'][a] = C(a', a)).  zs[g] is the
+// packed index of (g, 0, 0) and qb[q][r] the b of row-in-slab r of a slab with
+// q = lp - g, so that decoding t needs no arithmetic series.
+__device__ void recentre_x(const PairBuf &pb, ff tc, ff *out, const float (*bin)[kNPow], const int *zs,
+                           const unsigned char (*qb)[NPAIR_MAX + 2], int t0, int nt) {
     const int lp = pb.p.lp;
     const int nc = ncoef(lp);
     for (int t = (int)threadIdx.x - t0; t < nc; t += nt) {
-        int g = 0, b = 0, r = t;
-        for (g = 0; g <= lp; g++) {
-            const int cnt = ((lp - g + 1) * (lp - g + 2)) / 2;
-            if (r < cnt) break;
-            r -= cnt;
-        }
-        const int qn = lp - g;
-        for (b = 0; b <= qn; b++) {
-            if (r <= qn - b) break;
-            r -= qn - b + 1;
-        }
-        const int a = r, amax = lp - g - b;
+        int g = 0;
+        while (g < lp && zs[g + 1] <= t) g++;
+        const int qn = lp - g, r = t - zs[g];
+        const int b = qb[qn][r];
+        const int a = r - (b * (qn + 1) - (b * (b - 1)) / 2), amax = lp - g - b;
         const int base = t - a;  // packed index of (g, b, 0)
         ff s = {0.0f, 0.0f};
         for (int ap = amax; ap >= a; ap--) {
@@ -617,9 +619,10 @@ __device__ __forceinline__ uint32_t half_mask(uint32_t b) {
 
 // The NSL slices of one K = 16 operand row (v[k] for k < kNPow, zero beyond),
 // scaled by sc, as 16-byte chunks of 8 K values in the UMMA layout (planes of
-// plane_halves halves); K groups at or beyond kw are left as they are.
-__device__ __forceinline__ void slice_row16(const ff *vin, float sc, int kw, __half *plane0, int plane_halves,
-                                            int row) {
+// plane_halves halves); K groups at or beyond kw are left as they are, and those
+// at or beyond nval (v[k] == 0 for k >= nval) are written as zeros directly.
+__device__ __forceinline__ void slice_row16(const ff *vin, float sc, int kw, int nval, __half *plane0,
+                                            int plane_halves, int row) {
     // one compact loop body for both K groups: the second group's values are moved down
     ff v[8];
 #pragma unroll
@@ -627,6 +630,12 @@ __device__ __forceinline__ void slice_row16(const ff *vin, float sc, int kw, __h
 #pragma unroll 1
     for (int kg = 0; kg < KP / 8; kg++) {
         if (8 * kg >= kw) break;
+        if (8 * kg >= nval) {  // only zeros left: rewrite the stale slots without slicing
+            const int o16 = (row >> 3) * 16 + kg * 8 + (row & 7);
+#pragma unroll
+            for (int q = 0; q < NSL; q++) reinterpret_cast<uint4 *>(plane0 + q * plane_halves)[o16] = make_uint4(0, 0, 0, 0);
+            continue;
+        }
         uint32_t w[NSL][4];
 #pragma unroll
         for (int i = 0; i < 4; i++) {
@@ -826,6 +835,13 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
     const uint32_t idesc = tc::idesc_f16_f32(MROWS, TX);
     uint32_t phase = 0;
     for (int t = tid; t < kNPow * kNPow; t += NTHR) sm.bin[t / kNPow][t % kNPow] = c_binom[t / kNPow][t % kNPow];
+    // qb[L-1][pair_index(L, b, a)] = b: the (b, a) of a pair index without a search per use
+    for (int t = tid; t < kNPow * (NPAIR_MAX + 2); t += NTHR) {
+        const int Lq = t / (NPAIR_MAX + 2) + 1, q = t % (NPAIR_MAX + 2);
+        int b = 0, r = q;
+        while (b < Lq && r >= Lq - b) r -= Lq - b++;
+        sm.qb[Lq - 1][q] = (unsigned char)min(b, kNPow - 1);
+    }
     for (;;) {
         if (tid == 0) cm.tile = atomicAdd(A.queue, 1);
         __syncthreads();
@@ -877,35 +893,34 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
                     const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
                     // K slots beyond L may hold an earlier pair's slices: rewritten as zeros
-                    slice_row16(xv, sc, max(L, cm.kmax), sm.B[0], TX * KP, tid);
+                    slice_row16(xv, sc, max(L, cm.kmax), L, sm.B[0], TX * KP, tid);
                 } else if (warp == 1) {
                     build_yz(cm, P, Q, lv, td);
                 } else {
-                    recentre_x(pb, Q.tc, sm.rc, sm.bin, 64, NTHR - 64);
+                    // slab starts zs[g] = packed index of (g, 0, 0), then the re-expansion
+                    if (tid - 64 <= kNPow) sm.zs[tid - 64] = tid - 64 <= lp + 1 ? row_start(lp, tid - 64, 0) : 0;
+                    asm volatile("bar.sync 2, 64;" ::: "memory");
+                    recentre_x(pb, Q.tc, sm.rc, sm.bin, sm.zs, sm.qb, 64, NTHR - 64);
                 }
                 __syncthreads();
                 // stage 1: Cxy[z][(b,a)] = sum_g c'[g][b][a] Z[g][z]; one output per thread (16
-                // consecutive threads share (b, a)), two partial sums over even and odd g
+                // consecutive threads share (b, a)), two partial sums over even and odd g; the
+                // packed index of (g, b, a) is zs[g] - b g + k0
                 {
                     const int npair = (L * (L + 1)) / 2;
+                    const unsigned char *qbL = sm.qb[L - 1];
                     for (int t = tid; t < TZ * npair; t += NTHR) {
                         const int zz = t & (TZ - 1), q = t >> sh.lz;
-                        int b = 0, r = q;
-                        while (r >= L - b) {
-                            r -= L - b;
-                            b++;
-                        }
-                        const int a = r, n = lp - a - b;
-                        int off = row_start(lp, 0, b) + a;  // packed index of (g, b, a)
+                        const int b = qbL[q];
+                        const int a = q - (b * L - (b * (b - 1)) / 2), n = lp - a - b;
+                        const int k0 = b * (lp + 1) - (b * (b - 1)) / 2 + a;
                         ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
-                        int g = 0;
-                        for (; g + 1 <= n; g += 2) {
-                            const int off1 = off + ((lp - g + 1) * (lp - g + 2)) / 2 - b;
-                            s0 = ff_fma(sm.rc[off], cm.Z[g][zz], s0);
-                            s1 = ff_fma(sm.rc[off1], cm.Z[g + 1][zz], s1);
-                            off = off1 + ((lp - g) * (lp - g + 1)) / 2 - b;
+                        int g = 0, bg = 0;
+                        for (; g + 1 <= n; g += 2, bg += 2 * b) {
+                            s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
+                            s1 = ff_fma(sm.rc[sm.zs[g + 1] - bg - b + k0], cm.Z[g + 1][zz], s1);
                         }
-                        if (g <= n) s0 = ff_fma(sm.rc[off], cm.Z[g][zz], s0);
+                        if (g <= n) s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
                         sm.Cxy[zz][q] = ff_add(s0, s1);
                     }
                 }
@@ -922,24 +937,25 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 for (int a = 0; a < kNPow; a++) cx[a] = ff{0.0f, 0.0f};
                 float mx = 0.0f;
                 if (x0 <= x1) {
-                    // b outer (runtime), a inner unrolled with a warp-uniform exit at lp - b:
-                    // one compact loop body for every lp, up to kNPow independent updates
+                    // a in pairs (a0, a0 + 1; unrolled, uniform exit at lp), b inner (runtime
+                    // bound lp - a0): only the products that exist, two independent float-float
+                    // sums, each renormalised once at the end
                     const ff *crow = sm.Cxy[z];
-                    for (int b = 0; b <= lp; b++) {
-                        const ff yb = cm.Y[b][y];
-                        const ff *row = crow + pair_index(L, b, 0);
-                        const int n = lp - b;
-                        // chunks of 4 a: one uniform branch per chunk, selects inside (the
-                        // reads past the row stay inside Cxy and its padding)
 #pragma unroll
-                        for (int a0 = 0; a0 < kNPow; a0 += 4) {
-                            if (a0 > n) break;
-#pragma unroll
-                            for (int a = a0; a < a0 + 4 && a < kNPow; a++) {
-                                const ff t = ff_fma(row[a], yb, cx[a]);
-                                cx[a] = a <= n ? t : cx[a];
-                            }
+                    for (int a0 = 0; a0 < kNPow; a0 += 2) {
+                        if (a0 > lp) break;
+                        ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+                        const int nb = lp - a0;
+                        int q = a0;  // pair_index(L, b, a0); (b, a0 + 1) is q + 1
+#pragma unroll 1
+                        for (int b = 0; b <= nb; b++) {
+                            const ff yb = cm.Y[b][y];
+                            ff_acc_lazy(s0, crow[q], yb);
+                            if (b < nb) ff_acc_lazy(s1, crow[q + 1], yb);  // a0 + 1 + b <= lp
+                            q += L - b;
                         }
+                        cx[a0] = fast_two_sum(s0.hi, s0.lo);
+                        if (a0 + 1 < kNPow) cx[a0 + 1] = fast_two_sum(s1.hi, s1.lo);
                     }
                     const int sb = Q.sb;
 #pragma unroll
@@ -955,7 +971,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     const float sc = em == kZeroExp ? 0.0f : pow2i(SLB - em);
                     // entries a > lp of cx are zero; K slots that may hold an earlier pair's
                     // values (below kmax) are rewritten
-                    slice_row16(cx, sc, max(L, cm.kmax), sm.A[0], MROWS * KP, m);
+                    slice_row16(cx, sc, max(L, cm.kmax), L, sm.A[0], MROWS * KP, m);
                 }
                 // stage 3 on the tensor cores: D_s = sum_{i+j=s} A_i B_j^T
                 tc::fence_async_smem();
@@ -988,12 +1004,16 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 // tcgen05.ld is warp-collective: chunk decisions are made per warp
                 if (__any_sync(0xffffffffu, x0 <= x1)) {
                     const float rs = pow2i(max(em - 2 * SLB, -126));
+                    // bits x0..x1 of the row: the points of this pair's sphere on the row
+                    const uint32_t rmask =
+                        x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));
                     // one chunk of 8 x per iteration (a compact loop body: instruction fetch is
-                    // the kernel's first stall); acc_hi[0..7] always holds the current chunk's
+                    // a stall of this kernel); acc_hi[0..7] always holds the current chunk's
                     // sums, rotated by 8 after each chunk (four rotations restore the order)
 #pragma unroll 1
                     for (int c = 0; c < TX / 8; c++) {
-                        if (__any_sync(0xffffffffu, x0 <= x1 && 8 * c <= x1 && 8 * c + 7 >= x0)) {
+                        const uint32_t mc = rmask >> (8 * c);
+                        if (__any_sync(0xffffffffu, (mc & 0xFFu) != 0u)) {
                             uint32_t r2[8], r3[8], r4[8], r5[8];
                             const float4 csa = reinterpret_cast<const float4 *>(sm.cs)[2 * c];
                             const float4 csb = reinterpret_cast<const float4 *>(sm.cs)[2 * c + 1];
@@ -1006,7 +1026,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
 #pragma unroll
                             for (int i = 0; i < 8; i++) {
                                 const int x = 8 * c + i;
-                                const bool in = x >= x0 && x <= x1;  // straight-line code: selects, no branches
+                                const bool in = (mc >> i) & 1u;  // straight-line code: selects, no branches
                                 // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
                                 // lo the exact remainder (fast two-sum), then an exact two-sum into
                                 // acc_hi: acc_lo then only gathers rounding errors and remainders,
@@ -1082,6 +1102,12 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
     const uint32_t tbase = cm.tmem + ((uint32_t)(warp * 32) << 16);
     const uint32_t idesc = tc::idesc_f16_f32(MROWS, KP);
     uint32_t phase = 0;
+    for (int t = tid; t < kNPow * (NPAIR_MAX + 2); t += NTHR) {
+        const int Lq = t / (NPAIR_MAX + 2) + 1, q = t % (NPAIR_MAX + 2);
+        int b = 0, r = q;
+        while (b < Lq && r >= Lq - b) r -= Lq - b++;
+        sm.qb[Lq - 1][q] = (unsigned char)min(b, kNPow - 1);
+    }
     // B rows alpha >= L are never written: start them finite (zero)
     for (int t = tid; t < (int)(sizeof(sm.B) / sizeof(uint4)); t += NTHR)
         reinterpret_cast<uint4 *>(&sm.B[0][0][0])[t] = make_uint4(0u, 0u, 0u, 0u);
@@ -1195,6 +1221,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                     }
                 } else if (warp == 1) {
                     if constexpr (!kGeneral) bar_arrive1(NTHR);
+                    if (tid - 32 <= kNPow) sm.zs[tid - 32] = tid - 32 <= lp + 1 ? row_start(lp, tid - 32, 0) : 0;
                     build_yz(cm, P, Q, lv, td);
                 } else if constexpr (!kGeneral) {
                     bar_sync1(NTHR);
@@ -1302,44 +1329,35 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                 // rows have this z (a warp barrier after the readout suffices)
                 const int lzw = 5 - sh.ly;  // log2 of the z values per warp
                 const int zbase = (warp * 32) >> sh.ly;
+                const unsigned char *qbL = sm.qb[L - 1];
                 for (int t = tid & 31; t < (npair << lzw); t += 32) {
                     const int zz = zbase + (t & ((1 << lzw) - 1));
-                    int q = t >> lzw, b = 0;
-                    while (q >= L - b) { q -= L - b; b++; }
-                    const int a = q;
+                    const int q = t >> lzw, b = qbL[q];  // q = pair_index(L, b, a)
+                    const int a = q - (b * L - (b * (b - 1)) / 2);
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
 #pragma unroll 2
                     for (int yy = 0; yy < TY; yy += 2) {
-                        s0 = ff_fma(sm.st.S[zz * TY + yy][a], cm.Y[b][yy], s0);
-                        s1 = ff_fma(sm.st.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1], s1);
+                        ff_acc_lazy(s0, sm.st.S[zz * TY + yy][a], cm.Y[b][yy]);
+                        ff_acc_lazy(s1, sm.st.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1]);
                     }
-                    sm.st.T[zz][pair_index(L, b, a)] = ff_add(s0, s1);
+                    sm.st.T[zz][q] = ff_add(s0, s1);
                 }
                 __syncthreads();
                 // stage 1 transposed: W[g][b][a] += sum_z T[z][(b,a)] Z[g][z]
                 const int nc = ncoef(lp);
                 for (int t = tid; t < nc; t += NTHR) {
-                    int g = 0, b = 0, a = 0;
-                    {
-                        int r = t;
-                        for (g = 0; g <= lp; g++) {
-                            const int cnt = ((lp - g + 1) * (lp - g + 2)) / 2;
-                            if (r < cnt) break;
-                            r -= cnt;
-                        }
-                        const int q = lp - g;
-                        for (b = 0; b <= q; b++) {
-                            if (r <= q - b) break;
-                            r -= q - b + 1;
-                        }
-                        a = r;
-                    }
+                    // (g, b, a) of packed index t: slab g by the slab starts, b by the pair table
+                    int g = 0;
+                    while (g < lp && sm.zs[g + 1] <= t) g++;
+                    const int qn = lp - g, r = t - sm.zs[g];
+                    const int b = sm.qb[qn][r];
+                    const int a = r - (b * (qn + 1) - (b * (b - 1)) / 2);
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
                     const int pi = pair_index(L, b, a);
 #pragma unroll 2
                     for (int zz = 0; zz < TZ; zz += 2) {
-                        s0 = ff_fma(sm.st.T[zz][pi], cm.Z[g][zz], s0);
-                        s1 = ff_fma(sm.st.T[zz + 1][pi], cm.Z[g][zz + 1], s1);
+                        ff_acc_lazy(s0, sm.st.T[zz][pi], cm.Z[g][zz]);
+                        ff_acc_lazy(s1, sm.st.T[zz + 1][pi], cm.Z[g][zz + 1]);
                     }
                     const ff s = ff_add(s0, s1);
                     if (s.hi != 0.0f) {
