@@ -125,7 +125,7 @@ def algorithmic_flops(wl) -> tuple:
     from libgpw_gb300 import tasks as T
 
     t = wl.tasks
-    L = (t["la_max"] + t["lb_max"] + 1 + 2 * wl.compute_tau).astype(np.float64)
+    L = (t["la_max"] + t["lb_max"] + 1 + 2 * (wl.compute_tau != 0)).astype(np.float64)
     n = np.zeros((t.shape[0], 3))
     for lev_i, g in enumerate(wl.levels):
         m = t["level"] == lev_i

@@ -25,7 +25,7 @@ extern "C" {
 
 #define GPW_MAX_LEVELS 8
 #define GPW_MAX_L 4          /* largest la_max / lb_max of one primitive    */
-#define GPW_MAX_LP 10        /* la_max + lb_max (+2 for tau)                 */
+#define GPW_MAX_LP 10        /* la_max + lb_max (+2 for the derivative functions) */
 
 enum gpw_status {
     GPW_SUCCESS = 0,
@@ -36,6 +36,26 @@ enum gpw_status {
     GPW_ERR_NO_DEVICE = 5,
     GPW_ERR_ALLOC = 6,
     GPW_ERR_TIMEOUT = 7        /* a bounded device wait gave up               */
+};
+
+/*
+ * The function of each pair that collocate maps onto the grid (and integrate
+ * takes the adjoint of), with phi_a, phi_b the pair's Cartesian Gaussians and
+ * P the density block:
+ *   GPW_FUNC_AB          sum P phi_a phi_b                 (rho, grid_base_ref_c.cc:158-192)
+ *   GPW_FUNC_DADB        sum P 1/2 grad phi_a . grad phi_b (tau, grid_base_ref_c.cc:65-155;
+ *                        compute_polynomial_coefficients_DADB, coefficient.hpp:67-196)
+ *   GPW_FUNC_ADBMDAB_X   sum P (phi_a d_x phi_b - d_x phi_a phi_b), and _Y, _Z
+ *                        (compute_polynomial_coefficients_ADBmDAB, coefficient.hpp:209-354,
+ *                        restated with accumulation throughout)
+ * The values 0 and 1 keep the meaning of the reference's compute_tau flag.
+ */
+enum gpw_function {
+    GPW_FUNC_AB = 0,
+    GPW_FUNC_DADB = 1,
+    GPW_FUNC_ADBMDAB_X = 2,
+    GPW_FUNC_ADBMDAB_Y = 3,
+    GPW_FUNC_ADBMDAB_Z = 4
 };
 
 /* Arithmetic of the cube contraction. */
@@ -120,12 +140,13 @@ int gpw_plan_destroy(gpw_plan *plan);
 /*
  * Uploads and analyses a task list (host memory) for repeated collocate /
  * integrate calls: validation, sorting by level and grid tile, per-tile work
- * lists.  compute_tau selects the kinetic-energy density (grid_base_ref_c.cc:889-900).
+ * lists.  func (enum gpw_function) selects the collocated function; 0 and 1
+ * are the reference's compute_tau = false / true (grid_base_ref_c.cc:889-900).
  * sphere_table (host, may be NULL) holds the CP2K-format lists that tasks with
  * sphere_offset >= 0 index.  Allocates device memory; synchronous.
  */
 int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks,
-                       int compute_tau, const int *sphere_table,
+                       int func, const int *sphere_table,
                        int64_t sphere_table_len, gpw_taskset **out);
 int gpw_taskset_destroy(gpw_taskset *ts);
 /* Number of elements the pab / hab buffer must hold for this task set. */

@@ -137,8 +137,14 @@ class Plan:
             pass
 
 
+# the collocated function of a task set (enum gpw_function): 0 rho, 1 tau, and
+# phi_a d phi_b - d phi_a phi_b along x, y, z
+FUNC = {"ab": 0, "dadb": 1, "adbmdab_x": 2, "adbmdab_y": 3, "adbmdab_z": 4}
+
+
 class TaskSet:
-    """Uploaded, sorted and binned pairs (gpw_taskset_create)."""
+    """Uploaded, sorted and binned pairs (gpw_taskset_create).  compute_tau is
+    the gpw_function of the task set (0 / 1: the reference's compute_tau)."""
 
     def __init__(self, plan: Plan, tasks, compute_tau: int = 0, sphere_table=None):
         self.plan = plan

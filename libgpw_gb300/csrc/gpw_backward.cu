@@ -10,6 +10,10 @@
 // with |a'| <= la_max + 2.  Those come from the moments of V against the product
 // Gaussian up to degree lp + 2 (one more integrate pass, the 1-D tables are
 // recomputed), re-centred on a and b with the binomials of grid_base_ref_c.cc:195-231.
+// The derivative functions (tau and phi_a d phi_b - d phi_a phi_b) are sums over
+// their local block P'(a', b') of P' phi_a' phi_b' (shells l +- 1, coefficients
+// that depend on the exponents): the same rule applies per local element, plus
+// dP'/dzeta I(a', b') for the exponent gradients.
 #include <cuda_runtime.h>
 
 #include "gpw_coef.cuh"
@@ -17,12 +21,12 @@
 
 namespace gpw {
 
-constexpr int kBI = kMaxL + 3;          // a' components up to la_max + 2
-constexpr int kBK = 2 * (kMaxL + 2) + 1;
+constexpr int kBI = kMaxL + 4;          // components up to l_max + 1 (local block) + 2
+constexpr int kBK = 2 * kBI - 1;
 
 struct BwdSmem {
     double al[3][kBI][kBI][kBK];
-    double W[286];
+    double W[(kNPowB * (kNPowB + 1) * (kNPowB + 2)) / 6];  // moments up to degree lp + 2
     double red[8][4];
 };
 
@@ -41,13 +45,13 @@ __device__ __forceinline__ double pair_integral(const BwdSmem &s, int lpe, const
 
 __global__ void __launch_bounds__(128)
 k_backward_epilogue(const PairGeom *__restrict__ geoms, const LevelDev *__restrict__ levels,
-                    const double *__restrict__ tmat, const double *__restrict__ mom_ext,
+                    const double *__restrict__ tmat, const double *__restrict__ mom_ext, int func,
                     const double *__restrict__ pab, double *dra, double *drb, double *dza, double *dzb) {
     __shared__ BwdSmem s;
     const PairGeom g = geoms[blockIdx.x];
     const int tid = threadIdx.x;
     const int lpe = g.lp + 2;
-    const int ia = g.la0_max + 2, jb = g.lb0_max + 2;
+    const int ia = g.la_max + 2, jb = g.lb_max + 2;  // local shells (after the function's shift)
     // re-centring binomials (x-a)^i (x-b)^j = sum_k al[i][j][k] (x-p)^k
     for (int t = tid; t < 3 * (ia + 1) * (jb + 1); t += blockDim.x) {
         const int j = t % (jb + 1), i = (t / (jb + 1)) % (ia + 1), ax = t / ((jb + 1) * (ia + 1));
@@ -99,15 +103,20 @@ k_backward_epilogue(const PairGeom *__restrict__ geoms, const LevelDev *__restri
     }
     __syncthreads();
     double grad[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // dRa[3], dRb[3], dza, dzb
-    const int na = ncoset(g.la0_max), nb = ncoset(g.lb0_max);
+    const int na = ncoset(g.la_max), nb = ncoset(g.lb_max);
     for (int t = tid; t < na * nb; t += blockDim.x) {
         const int jco = t / na, ico = t % na;
         int a[3], b[3];
         coset_decode(ico, a[0], a[1], a[2]);
         coset_decode(jco, b[0], b[1], b[2]);
-        const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
-        if (la < g.la0_min || la > g.la0_max || lb < g.lb0_min || lb > g.lb0_max) continue;
-        const double P = pab[block_index(g, jco, ico)];
+        double dPa, dPb;  // dP'/dzeta, dP'/dzetb of the local element
+        const double P = local_entry(g, func, pab, a, b, &dPa, &dPb);
+        if (P == 0.0 && dPa == 0.0 && dPb == 0.0) continue;
+        if (dPa != 0.0 || dPb != 0.0) {
+            const double I0 = pair_integral(s, lpe, a, b);
+            grad[6] += dPa * I0;
+            grad[7] += dPb * I0;
+        }
         if (P == 0.0) continue;
         for (int d = 0; d < 3; d++) {
             int a2[3] = {a[0], a[1], a[2]}, b2[3] = {b[0], b[1], b[2]};
@@ -164,7 +173,11 @@ cudaError_t launch_backward(const TaskSet &ts, const double *d_pab, const GridPt
                             double *d_dra, double *d_drb, double *d_dza, double *d_dzb, cudaStream_t s) {
     (void)d_hab;
     if (ts.ntasks == 0) return cudaSuccess;
-    if (ts.tau || ts.max_lp + 2 > kMaxLp) return cudaErrorNotSupported;
+    // orthorhombic moments go to degree lp + 2 <= kMaxLpB; general cells map them
+    // through the lattice transform, which is built to degree kMaxLp
+    for (int64_t k = ts.gen_first; k < ts.gen_first + ts.gen_count; k++)
+        if (ts.h_geom[k].lp + 2 > kMaxLp) return cudaErrorNotSupported;
+    if (ts.max_lp + 2 > kMaxLpB) return cudaErrorNotSupported;
     TaskSet &mts = const_cast<TaskSet &>(ts);
     if (!mts.d_mom_ext) {
         cudaError_t e = cudaMalloc(&mts.d_mom_ext, sizeof(double) * std::max<int64_t>(ts.mom_ext_len, 1));
@@ -174,7 +187,8 @@ cudaError_t launch_backward(const TaskSet &ts, const double *d_pab, const GridPt
     if (e != cudaSuccess) return e;
     ts.n_kernels++;
     k_backward_epilogue<<<(unsigned)ts.ntasks, 128, 0, s>>>(ts.d_geom, ts.plan->d_levels, ts.plan->d_tmat,
-                                                           mts.d_mom_ext, d_pab, d_dra, d_drb, d_dza, d_dzb);
+                                                           mts.d_mom_ext, ts.tau, d_pab, d_dra, d_drb, d_dza,
+                                                           d_dzb);
     return cudaGetLastError();
 }
 

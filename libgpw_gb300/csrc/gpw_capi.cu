@@ -118,7 +118,7 @@ int convert_list(const int *sb, int64_t avail, const int lb[3], const int ub[3],
 }
 
 // Host geometry of one pair (grid_base_ref_c.cc:878-900, :534-553, :636-726).
-int make_geom(const gpw_task &t, int idx, const Plan &P, int tau, const int *table, int64_t table_len,
+int make_geom(const gpw_task &t, int idx, const Plan &P, int func, const int *table, int64_t table_len,
               PairGeom &g, std::vector<int> &dev_table) {
     char buf[256];
     if (t.level < 0 || t.level >= P.nlevels) {
@@ -154,7 +154,7 @@ int make_geom(const gpw_task &t, int idx, const Plan &P, int tau, const int *tab
         g.rb[i] = t.ra[i] + t.rab[i];
     }
     g.la0_max = t.la_max; g.la0_min = t.la_min; g.lb0_max = t.lb_max; g.lb0_min = t.lb_min;
-    if (tau) {
+    if (func != GPW_FUNC_AB) {  // the derivative functions need shells l - 1 .. l + 1
         g.la_max = t.la_max + 1; g.la_min = std::max(t.la_min - 1, 0);
         g.lb_max = t.lb_max + 1; g.lb_min = std::max(t.lb_min - 1, 0);
     } else {
@@ -271,12 +271,12 @@ int level_from_desc(const gpw_grid_desc &d, LevelDev &v) {
 }
 
 // Host geometry of one pair on a single level (the task's level must be 0).
-int host_pair_geom(const gpw_task &t, int idx, const LevelDev &lv, int tau, PairGeom &g) {
+int host_pair_geom(const gpw_task &t, int idx, const LevelDev &lv, int func, PairGeom &g) {
     Plan P;
     P.nlevels = 1;
     P.lv[0] = lv;
     std::vector<int> no_table;
-    return make_geom(t, idx, P, tau, nullptr, 0, g, no_table);
+    return make_geom(t, idx, P, func, nullptr, 0, g, no_table);
 }
 
 void set_last_error(const std::string &msg) { fail(0, msg); }
@@ -400,16 +400,18 @@ int gpw_plan_destroy(gpw_plan *plan) {
     return GPW_SUCCESS;
 }
 
-int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, int compute_tau,
+int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, int func,
                        const int *sphere_table, int64_t sphere_table_len, gpw_taskset **out) {
     if (!plan || !out || (ntasks > 0 && !tasks) || ntasks < 0 || ntasks > INT32_MAX)
         return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_create: bad arguments");
+    if (func < GPW_FUNC_AB || func > GPW_FUNC_ADBMDAB_Z)
+        return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_create: func must be a gpw_function (0..4)");
     *out = nullptr;
     std::vector<PairGeom> geo((size_t)ntasks);
     std::vector<int> table;
     int64_t extent = 0;
     for (int64_t i = 0; i < ntasks; i++) {
-        int st = make_geom(tasks[i], (int)i, *plan, compute_tau ? 1 : 0, sphere_table, sphere_table_len,
+        int st = make_geom(tasks[i], (int)i, *plan, func, sphere_table, sphere_table_len,
                            geo[i], table);
         if (st) return st;
         const gpw_task &t = tasks[i];
@@ -433,7 +435,7 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
     T->plan = plan;
     for (int l = 0; l < GPW_MAX_LEVELS; l++)  // general-cell levels start on the float-float kernel
         T->tile_lz[l] = (l < plan->nlevels && !plan->lv[l].ortho) ? kUntiled : kDefaultTileLz;
-    T->tau = compute_tau ? 1 : 0;
+    T->tau = func;
     T->ntasks = ntasks;
     T->pab_extent = extent;
     T->h_geom.resize((size_t)ntasks);
@@ -444,7 +446,7 @@ int gpw_taskset_create(gpw_plan *plan, const gpw_task *tasks, int64_t ntasks, in
         g.coef_off = coef;
         coef += ncoef(g.lp);
         g.mom_ext_off = mom_ext;
-        mom_ext += ncoef(std::min(g.lp + 2, kMaxLp));
+        mom_ext += ncoef(g.lp + 2);
         T->max_lp = std::max(T->max_lp, g.lp);
         T->max_A = std::max(T->max_A, g.la_max);
         T->max_B = std::max(T->max_B, g.lb_max);
@@ -832,7 +834,7 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
     if (use_ortho)
         for (int i = 0; i < 3; i++) { t.lb_cube[i] = lb_cube[i]; t.ub_cube[i] = ub_cube[i]; }
     gpw_taskset *T = nullptr;
-    st = gpw_taskset_create(P, &t, 1, compute_tau, use_ortho ? sphere_bounds : nullptr,
+    st = gpw_taskset_create(P, &t, 1, compute_tau ? GPW_FUNC_DADB : GPW_FUNC_AB, use_ortho ? sphere_bounds : nullptr,
                             use_ortho ? nspheres : 0, &T);
     if (st == GPW_SUCCESS) {
         // the block is read at (o2+jco)*maxco + o1+ico < maxco*maxco

@@ -3,6 +3,8 @@
 // Forward (collocate set-up), following grid_base_ref_c.cc:849-979:
 //   density block  -> local block P(b,a)     rho: grid_base_ref_c.cc:158-192
 //                                             tau: grid_base_ref_c.cc:65-155
+//                                             phi_a d phi_b - d phi_a phi_b:
+//                                               coefficient.hpp:209-354 (restated)
 //   1-D re-centring (x-a)^i (x-b)^j = sum_k al[i][j][k] (x-p)^k   :195-231
 //   P -> c[lz][ly][lx] by three one-axis contractions              :234-315
 // Adjoint (integrate back-transform): the same three contractions transposed,
@@ -102,41 +104,77 @@ __device__ inline int64_t block_index(const PairGeom &g, int jco, int ico) {
     return g.pab_offset + (int64_t)(g.o2 + jco) * g.maxco + (g.o1 + ico);
 }
 
-// P(b', a') of the local block (rho copy or tau gradient products).
-__device__ inline void fill_local_block(CoefWs &w, const PairGeom &g, int tau, const double *pab) {
+// The density block element P(bs, as) if (as, bs) lies in the pair's shells, else 0.
+__device__ inline double block_entry(const PairGeom &g, const double *pab, const int as[3], const int bs[3]) {
+    const int las = as[0] + as[1] + as[2], lbs = bs[0] + bs[1] + bs[2];
+    if (las < g.la0_min || las > g.la0_max || lbs < g.lb0_min || lbs > g.lb0_max) return 0.0;
+    return pab[block_index(g, coset(bs[0], bs[1], bs[2]), coset(as[0], as[1], as[2]))];
+}
+
+// One element P'(b', a') of the local block of function `func` (gpw_function)
+// and, when dza / dzb are given, its derivatives with respect to the exponents.
+// With d/dx phi_a = l phi_{a - e} - 2 za phi_{a + e} (per axis):
+//   rho      P' = P
+//   tau      P'(a', b') = 1/2 sum_d sum over the two terms of each side
+//   ADBmDAB  phi_a d_d phi_b - d_d phi_a phi_b: P(a', b' + e_d)(b'_d + 1)
+//            - 2 zb P(a', b' - e_d) - (a'_d + 1) P(a' + e_d, b') + 2 za P(a' - e_d, b')
+__device__ inline double local_entry(const PairGeom &g, int func, const double *pab, const int a[3],
+                                     const int b[3], double *dza = nullptr, double *dzb = nullptr) {
+    double v = 0.0, va = 0.0, vb = 0.0;
+    if (func == GPW_FUNC_AB) {
+        v = block_entry(g, pab, a, b);
+    } else if (func == GPW_FUNC_DADB) {
+        for (int d = 0; d < 3; d++)
+            for (int sa = 0; sa < 2; sa++) {
+                int as[3] = {a[0], a[1], a[2]};
+                double ca, dca;
+                if (sa == 0) { as[d] += 1; ca = (double)as[d]; dca = 0.0; }  // source lowered to a'
+                else { if (a[d] == 0) continue; as[d] -= 1; ca = -2.0 * g.zeta; dca = -2.0; }  // source raised
+                for (int sb = 0; sb < 2; sb++) {
+                    int bs[3] = {b[0], b[1], b[2]};
+                    double cb, dcb;
+                    if (sb == 0) { bs[d] += 1; cb = (double)bs[d]; dcb = 0.0; }
+                    else { if (b[d] == 0) continue; bs[d] -= 1; cb = -2.0 * g.zetb; dcb = -2.0; }
+                    const double p = 0.5 * block_entry(g, pab, as, bs);
+                    v += ca * cb * p;
+                    va += dca * cb * p;
+                    vb += ca * dcb * p;
+                }
+            }
+    } else {
+        const int d = func - GPW_FUNC_ADBMDAB_X;
+        int as[3] = {a[0], a[1], a[2]}, bs[3] = {b[0], b[1], b[2]};
+        bs[d] = b[d] + 1;
+        v += (double)(b[d] + 1) * block_entry(g, pab, a, bs);
+        if (b[d] > 0) {
+            bs[d] = b[d] - 1;
+            const double p = block_entry(g, pab, a, bs);
+            v -= 2.0 * g.zetb * p;
+            vb -= 2.0 * p;
+        }
+        as[d] = a[d] + 1;
+        v -= (double)(a[d] + 1) * block_entry(g, pab, as, b);
+        if (a[d] > 0) {
+            as[d] = a[d] - 1;
+            const double p = block_entry(g, pab, as, b);
+            v += 2.0 * g.zeta * p;
+            va += 2.0 * p;
+        }
+    }
+    if (dza) *dza = va;
+    if (dzb) *dzb = vb;
+    return v;
+}
+
+// P(b', a') of the local block of function `func` (gpw_function).
+__device__ inline void fill_local_block(CoefWs &w, const PairGeom &g, int func, const double *pab) {
     const int n = w.d.n_P();
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         const int jco = t / w.d.nla, ico = t % w.d.nla;
         int a[3], b[3];
         coset_decode(ico, a[0], a[1], a[2]);
         coset_decode(jco, b[0], b[1], b[2]);
-        const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
-        double v = 0.0;
-        if (!tau) {
-            if (la >= g.la0_min && la <= g.la0_max && lb >= g.lb0_min && lb <= g.lb0_max)
-                v = pab[block_index(g, jco, ico)];
-        } else {
-            for (int d = 0; d < 3; d++)
-                for (int sa = 0; sa < 2; sa++) {
-                    int as[3] = {a[0], a[1], a[2]};
-                    double ca;
-                    if (sa == 0) { as[d] += 1; ca = (double)as[d]; }       // source lowered to a'
-                    else { if (a[d] == 0) continue; as[d] -= 1; ca = -2.0 * g.zeta; }  // source raised
-                    const int las = as[0] + as[1] + as[2];
-                    if (las < g.la0_min || las > g.la0_max) continue;
-                    for (int sb = 0; sb < 2; sb++) {
-                        int bs[3] = {b[0], b[1], b[2]};
-                        double cb;
-                        if (sb == 0) { bs[d] += 1; cb = (double)bs[d]; }
-                        else { if (b[d] == 0) continue; bs[d] -= 1; cb = -2.0 * g.zetb; }
-                        const int lbs = bs[0] + bs[1] + bs[2];
-                        if (lbs < g.lb0_min || lbs > g.lb0_max) continue;
-                        v += 0.5 * ca * cb *
-                             pab[block_index(g, coset(bs[0], bs[1], bs[2]), coset(as[0], as[1], as[2]))];
-                    }
-                }
-        }
-        w.P[t] = v;
+        w.P[t] = local_entry(g, func, pab, a, b);
     }
 }
 
@@ -194,7 +232,7 @@ __device__ inline void forward_coef(CoefWs &w, const PairGeom &g, double *out) {
 }
 
 // Adjoint: given moments W (packed like c), accumulate into hab.
-__device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int tau, const double *W,
+__device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int func, const double *W,
                                     double *hab) {
     const CoefDims &d = w.d;
     const int L = d.L, lp = g.lp;
@@ -250,8 +288,28 @@ __device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int tau, const
         const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
         if (la < g.la0_min || la > g.la0_max || lb < g.lb0_min || lb > g.lb0_max) continue;
         double s = 0.0;
-        if (!tau) {
+        auto Pl = [&](const int at[3], const int bt[3]) {
+            return w.P[coset(bt[0], bt[1], bt[2]) * d.nla + coset(at[0], at[1], at[2])];
+        };
+        if (func == GPW_FUNC_AB) {
             s = w.P[jco * d.nla + ico];
+        } else if (func >= GPW_FUNC_ADBMDAB_X) {
+            // the transpose of local_entry: source (a, b) feeds (a, b - e), (a, b + e),
+            // (a - e, b) and (a + e, b)
+            const int dd = func - GPW_FUNC_ADBMDAB_X;
+            int at[3] = {a[0], a[1], a[2]}, bt[3] = {b[0], b[1], b[2]};
+            if (b[dd] > 0) {
+                bt[dd] = b[dd] - 1;
+                s += (double)b[dd] * Pl(a, bt);
+            }
+            bt[dd] = b[dd] + 1;
+            s -= 2.0 * g.zetb * Pl(a, bt);
+            if (a[dd] > 0) {
+                at[dd] = a[dd] - 1;
+                s -= (double)a[dd] * Pl(at, b);
+            }
+            at[dd] = a[dd] + 1;
+            s += 2.0 * g.zeta * Pl(at, b);
         } else {
             for (int dd = 0; dd < 3; dd++)
                 for (int sa = 0; sa < 2; sa++) {

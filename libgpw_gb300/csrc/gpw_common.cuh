@@ -23,6 +23,9 @@ namespace gpw {
 constexpr int kMaxL = GPW_MAX_L;    // per primitive
 constexpr int kMaxLp = GPW_MAX_LP;  // la_max + lb_max (+2 with tau)
 constexpr int kNPow = kMaxLp + 1;
+// the backward pass needs moments two degrees beyond the forward coefficients
+constexpr int kMaxLpB = kMaxLp + 2;
+constexpr int kNPowB = kMaxLpB + 1;
 
 GPW_HD int ncoset(int l) { return l < 0 ? 0 : ((l + 1) * (l + 2) * (l + 3)) / 6; }
 GPW_HD int nshell(int l) { return ((l + 1) * (l + 2)) / 2; }

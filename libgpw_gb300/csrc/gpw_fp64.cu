@@ -234,9 +234,9 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
                 continue;
             }
             const int64_t rowbase = ((int64_t)k * lv.ngrid[1] + j) * lv.ngrid[0];
-            double acc[kNPow];
+            double acc[kNPowB];
 #pragma unroll
-            for (int lx = 0; lx < kNPow; lx++) acc[lx] = 0.0;
+            for (int lx = 0; lx < kNPowB; lx++) acc[lx] = 0.0;
             for (int ig = igmin + lane; ig <= 1 - igmin; ig += 32) {
                 const int i = axis_index(lv.periodic[0], g.cc[0], ig, g.lb[0], lv.lb_grid[0],
                                          lv.npts[0], lv.ngrid[0]);
@@ -252,14 +252,14 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
                 } else {
                     const double v = grid[rowbase + i];
 #pragma unroll
-                    for (int lx = 0; lx < kNPow; lx++)
+                    for (int lx = 0; lx < kNPowB; lx++)
                         if (lx < L) acc[lx] += v * Xi[lx * nx];
                 }
             }
             if (kAdj) {
                 // warp-shuffle reduction of the row moments
 #pragma unroll
-                for (int lx = 0; lx < kNPow; lx++) {
+                for (int lx = 0; lx < kNPowB; lx++) {
                     double v = acc[lx];
                     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                     acc[lx] = v;

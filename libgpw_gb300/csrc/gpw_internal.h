@@ -37,7 +37,7 @@ constexpr int kUntiled = -1;       // a general-cell level on the float-float ke
 
 struct TaskSet {
     Plan *plan = nullptr;
-    int tau = 0;
+    int tau = 0;                   // gpw_function of the task set (0: rho, 1: tau, 2-4: ADBmDAB x/y/z)
     int64_t ntasks = 0;
     int64_t pab_extent = 0;
     int max_lp = 0;

@@ -98,7 +98,7 @@ class Workload:
     tasks: np.ndarray                       # TASK_DTYPE[n]
     levels: list                            # GRID_DTYPE scalars
     pab: np.ndarray                         # float64[extent]
-    compute_tau: int = 0
+    compute_tau: int = 0                    # gpw_function: 0 rho, 1 tau, 2-4 ADBmDAB x/y/z
     sphere_table: np.ndarray | None = None  # int32, CP2K-format lists
     meta: dict = field(default_factory=dict)
 

@@ -79,10 +79,12 @@ static void pair_setup(int tau, int la_max, int la_min, int lb_max, int lb_min, 
 
 /* ------------------------------------------------------------------------- */
 /* Density block -> local block.  loc[jco][ico] with ld = ncoset(la_max_local).
- * rho: copy of the [la_min,la_max] x [lb_min,lb_max] shells (grid_base_ref_c.cc:158-192).
- * tau: 1/2 grad(a).grad(b) by d/dx x^l e^{-z x^2} = l x^{l-1} - 2 z x^{l+1}
- *      (grid_base_ref_c.cc:65-155).  `adj` runs the transposed map:
- *      block[...] += M^T loc.                                                   */
+ * func 0, rho: copy of the [la_min,la_max] x [lb_min,lb_max] shells (grid_base_ref_c.cc:158-192).
+ * func 1, tau: 1/2 grad(a).grad(b) by d/dx x^l e^{-z x^2} = l x^{l-1} - 2 z x^{l+1}
+ *      (grid_base_ref_c.cc:65-155; compute_polynomial_coefficients_DADB, coefficient.hpp:67-196).
+ * func 2, 3, 4: phi_a d_d phi_b - d_d phi_a phi_b along x, y, z by the same rule
+ *      (compute_polynomial_coefficients_ADBmDAB, coefficient.hpp:209-354, with every
+ *      term accumulated).  `adj` runs the transposed map: block[...] += M^T loc.     */
 static void block_map(int tau, int adj, int la_max, int la_min, int lb_max, int lb_min,
                       double zeta, double zetb, const double *blk, double *blk_out, int maxco,
                       int o1, int o2, double *loc, const double *loc_in, int ldl) {
@@ -105,6 +107,23 @@ static void block_map(int tau, int adj, int la_max, int la_min, int lb_max, int 
             int a[3] = {lxa, lya, lza}, b[3] = {lxb, lyb, lzb};
             double acc = 0.0;
             double p = adj ? 0.0 : blk[bidx];
+            if (tau >= 2) {
+                /* (a, b - e): b_d;  (a, b + e): -2 zetb;  (a - e, b): -a_d;  (a + e, b): 2 zeta */
+                int d = tau - 2;
+                for (int k = 0; k < 4; k++) {
+                    int a2[3] = {a[0], a[1], a[2]}, b2[3] = {b[0], b[1], b[2]};
+                    double w;
+                    if (k == 0) { if (b[d] == 0) continue; b2[d] -= 1; w = (double)b[d]; }
+                    else if (k == 1) { b2[d] += 1; w = -2.0 * zetb; }
+                    else if (k == 2) { if (a[d] == 0) continue; a2[d] -= 1; w = -(double)a[d]; }
+                    else { a2[d] += 1; w = 2.0 * zeta; }
+                    int ic2 = coset(a2[0], a2[1], a2[2]), jc2 = coset(b2[0], b2[1], b2[2]);
+                    if (!adj) loc[jc2 * ldl + ic2] += w * p;
+                    else acc += w * loc_in[jc2 * ldl + ic2];
+                }
+                if (adj) blk_out[bidx] += acc;
+                continue;
+            }
             for (int d = 0; d < 3; d++) {
                 /* two terms from each side: lower (coefficient l) and raise (-2 zeta) */
                 for (int sa = 0; sa < 2; sa++) {

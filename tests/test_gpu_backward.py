@@ -1,6 +1,7 @@
 """Backward kernels: dE/dpab (= integrate), forces dE/dRa, dE/dRb and exponent
 gradients dE/dzeta, dE/dzetb against FP64 central finite differences (h = 1e-5)
-of the CPU oracle's energy, <= 1e-6 relative."""
+of the CPU oracle's energy, <= 1e-6 relative, for rho, tau and
+phi_a d_x phi_b - d_x phi_a phi_b (gpw_function 0, 1, 2)."""
 import numpy as np
 import pytest
 
@@ -12,7 +13,13 @@ H = 1e-5
 TOL = 1e-6
 
 
-def workload(ortho=True, n=10, seed=41):
+def workload(ortho=True, n=10, seed=41, func=0):
+    wl = _workload(ortho, n, seed)
+    wl.compute_tau = func
+    return wl
+
+
+def _workload(ortho, n, seed):
     if ortho:
         wl = T.synthetic("bwd", n, 2, (0.3, 20.0), 8.0, [(40, 40, 40)], seed=seed)
     else:
@@ -79,12 +86,13 @@ def stable(O, wl, i):
     return True
 
 
+@pytest.mark.parametrize("func", [0, 1, 2])
 @pytest.mark.parametrize("ortho", [True, False])
-def test_forces_and_exponents_vs_fd(ortho, oracle_lib):
+def test_forces_and_exponents_vs_fd(ortho, func, oracle_lib):
     import torch
 
     O = oracle_lib
-    wl = workload(ortho)
+    wl = workload(ortho, func=func)
     V = wl.potentials(seed=6)
     dev = torch.device("cuda:0")
     plan = capi.Plan(wl.levels)
@@ -158,10 +166,14 @@ def test_autograd_function(oracle_lib):
     assert torch.all(torch.isfinite(gra)) and torch.all(torch.isfinite(gza))
 
 
-def test_backward_rejects_tau():
+def test_backward_tau_high_l_general_cell_rejected():
+    """tau with la = lb = 4 needs moments to degree 12; on a general cell they go
+    through the lattice transform, built to degree 10: reported, not computed."""
     import torch
 
-    wl = workload(True, n=3)
+    wl = T.synthetic("bwd_g4", 3, 4, (0.5, 20.0), T.lattice_15(length=8.0), [(36, 36, 36)], seed=2,
+                     ortho=False, lmin=4)
+    wl.tasks["radius"] = np.minimum(wl.tasks["radius"], 3.0)
     wl.compute_tau = 1
     plan = capi.Plan(wl.levels)
     ts = capi.TaskSet.from_workload(plan, wl)

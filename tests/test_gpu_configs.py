@@ -88,51 +88,8 @@ def test_1m_pair_workload_sample_tau():
 
 # ---------------------------------------------------------------------------
 # differentiation workload: forces and exponent gradients vs central differences
-H = 1e-5
 TOLF = 1e-6
 NSAMPLE = 60
-
-
-def _variants(wl, idx):
-    """Per sampled pair: the pair itself and its 16 central-difference variants
-    (ra, rb +-h along x, y, z; zeta, zetb +-h), each with its own copy of the
-    density block, as one Workload for one oracle call."""
-    t0 = wl.tasks
-    nsa = t0["maxco"].astype(np.int64)
-    nsb = ((t0["lb_max"] + 1) * (t0["lb_max"] + 2) // 2).astype(np.int64)
-    rows, blocks = [], []
-    for i in idx:
-        ra = t0["ra"][i].copy()
-        rb = ra + t0["rab"][i]
-        za, zb = float(t0["zeta"][i]), float(t0["zetb"][i])
-        var = [dict()]
-        for d in range(3):
-            e = np.zeros(3)
-            e[d] = H
-            var += [dict(ra=ra + e), dict(ra=ra - e), dict(rb=rb + e), dict(rb=rb - e)]
-        var += [dict(za=za + H), dict(za=za - H), dict(zb=zb + H), dict(zb=zb - H)]
-        blk = wl.pab[int(t0["pab_offset"][i]): int(t0["pab_offset"][i]) + int(nsa[i] * nsb[i])]
-        for v in var:
-            t = t0[i:i + 1].copy()
-            a = v.get("ra", ra)
-            b = v.get("rb", rb)
-            t["ra"][0] = a
-            t["rab"][0] = b - a
-            t["zeta"][0] = v.get("za", za)
-            t["zetb"][0] = v.get("zb", zb)
-            rows.append(t)
-            blocks.append(blk)
-    tasks = np.concatenate(rows)
-    off = np.zeros(len(blocks), np.int64)
-    off[1:] = np.cumsum([b.size for b in blocks[:-1]])
-    tasks["pab_offset"] = off
-    return T.Workload("fd", tasks, wl.levels, np.concatenate(blocks)), off, [b.size for b in blocks]
-
-
-def _cube_centre(t, h):
-    zp = t["zeta"] + t["zetb"]
-    rp = t["ra"] + (t["zetb"] / zp)[:, None] * t["rab"]
-    return np.floor(rp / h[None, :]).astype(np.int64)
 
 
 def test_differentiation_workload_forces_vs_fd():
@@ -142,54 +99,20 @@ def test_differentiation_workload_forces_vs_fd():
     a pair's point set is fixed by its cube centre; a pair whose centre moves
     under a step would make the difference quotient meaningless, so such pairs
     are skipped, and at most 5% may be."""
-    import torch
-
+    from fd_util import fd_gradients, gpu_gradients
     from oracle import oracle as O
 
     wl = T.config(4)
     V = wl.potentials(seed=6)
-    dev = torch.device("cuda:0")
-    plan = capi.Plan(wl.levels)
-    ts = capi.TaskSet.from_workload(plan, wl)
-    n = wl.ntasks
-    pab = torch.from_numpy(wl.pab).to(dev)
-    Vd = [torch.from_numpy(v).to(dev) for v in V]
-    hab = torch.zeros_like(pab)
-    dra = torch.zeros((n, 3), dtype=torch.float64, device=dev)
-    drb = torch.zeros_like(dra)
-    dza = torch.zeros(n, dtype=torch.float64, device=dev)
-    dzb = torch.zeros_like(dza)
-    ts.backward(pab, Vd, hab, dra, drb, dza, dzb)
-    ts.check()
-    dra, drb, dza, dzb = (x.cpu().numpy() for x in (dra, drb, dza, dzb))
-    idx = np.sort(np.random.default_rng(404).choice(n, size=NSAMPLE, replace=False))
-    fdw, off, size = _variants(wl, idx)
-    hab_v = O.batch(fdw, V=V, nthreads=NTHR)
-    E = np.array([float(np.dot(hab_v[o:o + s], fdw.pab[o:o + s])) for o, s in zip(off, size)]).reshape(NSAMPLE, 17)
-    h = np.diag(np.asarray(wl.levels[0]["dh"]))
-    cc = _cube_centre(fdw.tasks, h).reshape(NSAMPLE, 17, 3)
-    stable = np.all(cc == cc[:, :1, :], axis=(1, 2))
+    hab, grads = gpu_gradients(wl, V)
+    idx = np.sort(np.random.default_rng(404).choice(wl.ntasks, size=NSAMPLE, replace=False))
+    fd, stable = fd_gradients(O, wl, V, idx, nthreads=NTHR)
     assert stable.mean() >= 0.95, f"{(~stable).sum()} of {NSAMPLE} pairs change cube centre under a step"
-    checked = 0
     for s, i in enumerate(idx):
         if not stable[s]:
             continue
-        e = E[s]
-        fd = {}
-        for d in range(3):
-            fd[("ra", d)] = (e[1 + 4 * d] - e[2 + 4 * d]) / (2 * H)
-            fd[("rb", d)] = (e[3 + 4 * d] - e[4 + 4 * d]) / (2 * H)
-        fd[("za", 0)] = (e[13] - e[14]) / (2 * H)
-        fd[("zb", 0)] = (e[15] - e[16]) / (2 * H)
-        got = {("ra", d): dra[i, d] for d in range(3)}
-        got.update({("rb", d): drb[i, d] for d in range(3)})
-        got[("za", 0)] = dza[i]
-        got[("zb", 0)] = dzb[i]
-        scale = max(abs(v) for v in fd.values())  # 0 only where the prefactor underflows
-        for k in fd:
-            assert abs(got[k] - fd[k]) <= TOLF * scale, (i, k, got[k], fd[k])
-        checked += 1
-    assert checked >= int(0.95 * NSAMPLE)
+        scale = np.abs(fd[s]).max()  # 0 only where the prefactor underflows
+        assert np.all(np.abs(grads[i] - fd[s]) <= TOLF * scale), (i, grads[i], fd[s])
     # dE/dpab of the whole workload is the oracle's integrate
     want = O.batch(wl, V=V, nthreads=NTHR)
-    assert _max_rel(hab.cpu().numpy(), want) <= TOL64
+    assert _max_rel(hab, want) <= TOL64
