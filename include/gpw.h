@@ -186,6 +186,22 @@ int gpw_backward(gpw_taskset *ts, const double *d_pab, double *const *d_grids,
 int gpw_taskset_check(gpw_taskset *ts, void *stream);
 
 /*
+ * New centres and exponents for the same pairs (a geometry step of a force or
+ * molecular-dynamics loop), without rebuilding the task set: d_ra and d_rab
+ * (double[3 * ntasks]) and d_zeta, d_zetb (double[ntasks]) are device arrays in
+ * the task order given to gpw_taskset_create; a NULL array keeps the current
+ * values.  The pair set-up (zeta_p, prefactor, product centre, cube or box
+ * placement; grid_base_ref_c.cc:878-886) runs on the device in FP64 and the
+ * tiled path's bins are rebuilt on the device.  Radii, shells, cube lists and
+ * the density-block layout stay as created.  Synchronous; no launch of the task
+ * set may be in flight.  On an error (non-finite or non-positive inputs, a cube
+ * that would leave a non-periodic window) the task set is left unchanged.
+ * No reference counterpart: the reference sets a pair up on every call.
+ */
+int gpw_taskset_update_geometry(gpw_taskset *ts, const double *d_ra, const double *d_rab,
+                                const double *d_zeta, const double *d_zetb, void *stream);
+
+/*
  * Profiling counters of a task set, for benchmarks.  With enable != 0 the
  * library brackets each cube-contraction launch with CUDA events on the
  * launching stream.  gpw_taskset_stats waits for the device, returns the

@@ -59,6 +59,7 @@ def lib():
         "gpw_integrate": ([vp, i32, vp, vp, vp], i32),
         "gpw_backward": ([vp, vp, vp, vp, vp, vp, vp, vp, vp], i32),
         "gpw_taskset_check": ([vp, vp], i32),
+        "gpw_taskset_update_geometry": ([vp, vp, vp, vp, vp, vp], i32),
         "gpw_collocate_host": ([vp, i32, vp, vp], i32),
         "gpw_integrate_host": ([vp, i32, vp, vp], i32),
         "gpw_collocate_pgf_product_rspace": ([i32] * 6 + [dbl] * 3 + [vp] * 8 + [i32, dbl, vp, vp, i32, vp, i32,
@@ -195,6 +196,16 @@ class TaskSet:
         p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
         check(lib().gpw_backward(self.handle, pab.data_ptr(), self._ptrs(grids), p(hab), p(dra), p(drb), p(dzeta),
                                  p(dzetb), _stream_handle(stream)), "gpw_backward")
+
+    def update_geometry(self, ra=None, rab=None, zeta=None, zetb=None, stream=None):
+        """New centres / exponents of the same pairs (device tensors in task order;
+        None keeps the current values): gpw_taskset_update_geometry."""
+        p = lambda t: None if t is None else t.data_ptr()  # noqa: E731
+        for t in (ra, rab, zeta, zetb):
+            assert t is None or (t.is_cuda and t.dtype.is_floating_point and t.element_size() == 8
+                                 and t.is_contiguous())
+        check(lib().gpw_taskset_update_geometry(self.handle, p(ra), p(rab), p(zeta), p(zetb),
+                                                _stream_handle(stream)), "gpw_taskset_update_geometry")
 
     def profile(self, enable: bool = True):
         check(lib().gpw_taskset_profile(self.handle, int(enable)), "gpw_taskset_profile")

@@ -144,6 +144,8 @@ int make_geom(const gpw_task &t, int idx, const Plan &P, int func, const int *ta
     g.ortho = lv.ortho;
     g.zeta = t.zeta;
     g.zetb = t.zetb;
+    g.rscale = t.rscale;
+    for (int i = 0; i < 3; i++) g.rab[i] = t.rab[i];
     g.zetp = t.zeta + t.zetb;
     const double f = t.zetb / g.zetp;
     const double rab2 = t.rab[0] * t.rab[0] + t.rab[1] * t.rab[1] + t.rab[2] * t.rab[2];
@@ -221,6 +223,7 @@ int make_geom(const gpw_task &t, int idx, const Plan &P, int func, const int *ta
         for (int d = 0; d < 3; d++) {
             g.cc[d] = imin[d];
             g.hi[d] = imax[d];
+            g.ext0[d] = imax[d] - imin[d] + 1;
             if (!lv.periodic[d] && imax[d] - imin[d] + imod(imin[d] + lv.lb_grid[d], lv.npts[d]) >= lv.ngrid[d]) {
                 snprintf(buf, sizeof buf, "task %d: box leaves the local grid on non-periodic axis %d", idx, d);
                 return fail(GPW_ERR_OUT_OF_WINDOW, buf);
@@ -229,6 +232,87 @@ int make_geom(const gpw_task &t, int idx, const Plan &P, int func, const int *ta
         g.cost = (int64_t)(imax[0] - imin[0] + 1) * (imax[1] - imin[1] + 1) * (imax[2] - imin[2] + 1);
     }
     return GPW_SUCCESS;
+}
+
+// New centres and exponents for the pairs of a task set, on the device: the pair
+// set-up of make_geom (grid_base_ref_c.cc:878-886 and the cube / box placement)
+// with round-to-nearest arithmetic in the host's operation order, so that cube
+// centres and boxes land exactly where the host (and the oracle) put them.
+// Writes the updated geometry to `out`; flags kStatBadGeom for non-finite or
+// non-positive inputs and boxes the task set was not planned for, and
+// kStatOutOfWindow for cubes that leave a non-periodic window.
+__global__ void k_update_geom(const PairGeom *__restrict__ in, PairGeom *__restrict__ out, int64_t n,
+                              const LevelDev *__restrict__ levels, const double *__restrict__ ra,
+                              const double *__restrict__ rab, const double *__restrict__ zeta,
+                              const double *__restrict__ zetb, int *status) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        PairGeom g = in[k];
+        const int64_t t = g.task;
+        const LevelDev &lv = levels[g.level];
+        if (ra)
+            for (int i = 0; i < 3; i++) g.ra[i] = ra[3 * t + i];
+        if (rab)
+            for (int i = 0; i < 3; i++) g.rab[i] = rab[3 * t + i];
+        if (zeta) g.zeta = zeta[t];
+        if (zetb) g.zetb = zetb[t];
+        bool ok = g.zeta > 0.0 && g.zetb > 0.0 && isfinite(g.zeta) && isfinite(g.zetb);
+        for (int i = 0; i < 3; i++) ok = ok && isfinite(g.ra[i]) && isfinite(g.rab[i]);
+        if (!ok) {
+            atomicOr(status, kStatBadGeom);
+            out[k] = in[k];
+            continue;
+        }
+        g.zetp = radd(g.zeta, g.zetb);
+        const double f = rdiv(g.zetb, g.zetp);
+        const double rab2 = radd(radd(rmul(g.rab[0], g.rab[0]), rmul(g.rab[1], g.rab[1])), rmul(g.rab[2], g.rab[2]));
+        g.prefactor = rmul(g.rscale, exp(rmul(rmul(-g.zeta, f), rab2)));
+        for (int i = 0; i < 3; i++) {
+            g.rp[i] = radd(g.ra[i], rmul(f, g.rab[i]));
+            g.rb[i] = radd(g.ra[i], g.rab[i]);
+        }
+        if (g.ortho) {
+            for (int i = 0; i < 3; i++) {
+                double sdi = 0.0;
+                for (int j = 0; j < 3; j++) sdi = radd(sdi, rmul(lv.dh_inv[j][i], g.rp[j]));
+                g.cc[i] = (int)floor(sdi);
+                g.off[i] = rsub(g.rp[i], rmul((double)g.cc[i], lv.dh[i][i]));
+            }
+            for (int d = 0; d < 3; d++) {
+                if (lv.periodic[d]) continue;
+                const int a = axis_index(0, g.cc[d], g.lb[d], g.lb[d], lv.lb_grid[d], lv.npts[d], lv.ngrid[d]);
+                const int b = axis_index(0, g.cc[d], g.hi[d], g.lb[d], lv.lb_grid[d], lv.npts[d], lv.ngrid[d]);
+                if (a < 0 || b < 0) atomicOr(status, kStatOutOfWindow);
+            }
+        } else {
+            for (int i = 0; i < 3; i++) {
+                double sdi = 0.0;
+                for (int j = 0; j < 3; j++) sdi = radd(sdi, rmul(lv.dh_inv[j][i], g.rp[j]));
+                g.off[i] = sdi;
+            }
+            int imin[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, imax[3] = {INT32_MIN, INT32_MIN, INT32_MIN};
+            for (int a = -1; a <= 1; a++)
+                for (int b = -1; b <= 1; b++)
+                    for (int c = -1; c <= 1; c++) {
+                        const double x = radd(g.rp[0], rmul((double)a, g.radius));
+                        const double y = radd(g.rp[1], rmul((double)b, g.radius));
+                        const double z = radd(g.rp[2], rmul((double)c, g.radius));
+                        for (int d = 0; d < 3; d++) {
+                            const double sd = radd(radd(rmul(lv.dh_inv[0][d], x), rmul(lv.dh_inv[1][d], y)),
+                                                   rmul(lv.dh_inv[2][d], z));
+                            imin[d] = min(imin[d], (int)floor(sd));
+                            imax[d] = max(imax[d], (int)ceil(sd));
+                        }
+                    }
+            for (int d = 0; d < 3; d++) {
+                g.cc[d] = imin[d];
+                g.hi[d] = imax[d];
+                if (imax[d] - imin[d] + 1 > g.ext0[d] + 1) atomicOr(status, kStatBadGeom);
+                if (!lv.periodic[d] && imax[d] - imin[d] + imod(imin[d] + lv.lb_grid[d], lv.npts[d]) >= lv.ngrid[d])
+                    atomicOr(status, kStatOutOfWindow);
+            }
+        }
+        out[k] = g;
+    }
 }
 
 GridPtrs grid_ptrs(const Plan &P, double *const *p) {
@@ -538,6 +622,7 @@ int gpw_taskset_destroy(gpw_taskset *ts) {
     mixed_free(*ts);
     for (cudaEvent_t e : ts->ev_pool) cudaEventDestroy(e);
     cudaFree(ts->d_geom);
+    cudaFree(ts->d_geom_next);
     cudaFree(ts->d_table);
     cudaFree(ts->d_coef);
     cudaFree(ts->d_mom);
@@ -619,6 +704,42 @@ int gpw_taskset_check(gpw_taskset *ts, void *stream) {
     return GPW_SUCCESS;
 }
 
+int gpw_taskset_update_geometry(gpw_taskset *ts, const double *d_ra, const double *d_rab, const double *d_zeta,
+                                const double *d_zetb, void *stream) {
+    if (!ts) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_update_geometry: null task set");
+    if (ts->ntasks == 0) return GPW_SUCCESS;
+    GPW_CUDA(cudaSetDevice(ts->plan->device));
+    GPW_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    GPW_CUDA(cudaDeviceSynchronize());  // no launch of this task set may still read its geometry
+    if (!ts->d_geom_next) GPW_CUDA(cudaMalloc(&ts->d_geom_next, sizeof(PairGeom) * (size_t)ts->ntasks));
+    GPW_CUDA(cudaMemset(ts->d_status, 0, sizeof(int)));
+    const unsigned nblk = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ts->ntasks + 127) / 128, 8192));
+    k_update_geom<<<nblk, 128>>>(ts->d_geom, ts->d_geom_next, ts->ntasks, ts->plan->d_levels, d_ra, d_rab, d_zeta,
+                                 d_zetb, ts->d_status);
+    GPW_CUDA(cudaGetLastError());
+    int h = 0;
+    GPW_CUDA(cudaMemcpy(&h, ts->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    GPW_CUDA(cudaMemset(ts->d_status, 0, sizeof(int)));
+    if (h & kStatBadGeom)
+        return fail(GPW_ERR_INVALID_ARG,
+                    "gpw_taskset_update_geometry: exponents must be positive and finite, positions finite; "
+                    "the task set is unchanged");
+    if (h & kStatOutOfWindow)
+        return fail(GPW_ERR_OUT_OF_WINDOW,
+                    "gpw_taskset_update_geometry: a cube would leave the local grid; the task set is unchanged");
+    std::swap(ts->d_geom, ts->d_geom_next);
+    ts->h_geom_stale = true;
+    if (ts->mixed) {
+        std::string err;
+        const int st = mixed_rebin(*ts, err);
+        if (st) {
+            mixed_free(*ts);  // mixed calls then report GPW_ERR_UNSUPPORTED
+            return fail(st, err);
+        }
+    }
+    return GPW_SUCCESS;
+}
+
 // tz 4 / 8: tiles of that z extent; 0 (general-cell levels only): no tiles, the float-float kernel
 static int tile_lz_of(int tz, bool ortho) { return tz == 4 ? 2 : tz == 8 ? 3 : (tz == 0 && !ortho) ? kUntiled : -2; }
 static int tile_z_of(int lz) { return lz == kUntiled ? 0 : 1 << lz; }
@@ -629,6 +750,11 @@ static int retile(gpw_taskset *ts, const int *lz) {
     if (same && ts->mixed) return GPW_SUCCESS;
     GPW_CUDA(cudaSetDevice(ts->plan->device));
     GPW_CUDA(cudaDeviceSynchronize());  // the binned state may be in use by earlier launches
+    if (ts->h_geom_stale && ts->ntasks > 0) {  // the host copy after a device geometry update
+        GPW_CUDA(cudaMemcpy(ts->h_geom.data(), ts->d_geom, sizeof(PairGeom) * (size_t)ts->ntasks,
+                            cudaMemcpyDeviceToHost));
+        ts->h_geom_stale = false;
+    }
     mixed_free(*ts);
     for (int l = 0; l < ts->plan->nlevels; l++) ts->tile_lz[l] = lz[l];
     std::string err;

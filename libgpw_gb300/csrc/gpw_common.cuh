@@ -182,6 +182,10 @@ struct PairGeom {
     int64_t cost;      // estimated cube points
     int64_t mom_ext_off; // scratch offset of the degree lp+2 moments (backward)
     double zeta, zetb;
+    double rscale;
+    double rab[3];
+    int ext0[3];       // general: the box extents the task set was planned with
+    int pad_;
 };
 
 // Device status bits (OR-ed by kernels, read by gpw_taskset_check).
@@ -191,6 +195,7 @@ enum : int {
     kStatBadTable = 4,
     kStatTooManyImages = 8,
     kStatBadTile = 16,
+    kStatBadGeom = 32,      // a geometry update that the task set cannot take
 };
 
 }  // namespace gpw

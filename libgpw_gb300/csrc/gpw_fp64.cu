@@ -292,9 +292,10 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
 
 // ---------------------------------------------------------------------------
 // general cell, one CTA per pair (row bounds: general_row, gpw_common.cuh)
+// (one row of margin: a geometry update moves a box's extent by at most one)
 int smem_general_fp64(const PairGeom &g, int extra) {
     const int L = g.lp + 1 + extra;
-    const int ny = g.hi[1] - g.cc[1] + 1;
+    const int ny = g.hi[1] - g.cc[1] + 2;
     return 8 * (L * L * L + L * L + ny * L) + 12 * ny;
 }
 
@@ -681,7 +682,7 @@ static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool a
 // general-cell pairs of a mixed call: the float-float kernel
 int smem_general_ff(const PairGeom &g) {
     const int L = g.lp + 1;
-    const int ny = g.hi[1] - g.cc[1] + 1;
+    const int ny = g.hi[1] - g.cc[1] + 2;  // one row of margin, as smem_general_fp64
     return 8 * (L * L * L + L * L + 2 * ny * L + 3 * ny) + 12 * ny;
 }
 

@@ -42,8 +42,10 @@ struct TaskSet {
     int64_t pab_extent = 0;
     int max_lp = 0;
     int max_A = 0, max_B = 0;
-    std::vector<PairGeom> h_geom;  // sorted
+    std::vector<PairGeom> h_geom;  // sorted (stale after a device geometry update until refreshed)
+    bool h_geom_stale = false;
     PairGeom *d_geom = nullptr;
+    PairGeom *d_geom_next = nullptr;  // geometry updates are written here, then swapped in
     int *d_table = nullptr;        // random-access cube lists (explicit tables)
     double *d_coef = nullptr;      // packed coefficients, per call
     double *d_mom = nullptr;       // packed moments (integrate), per call
@@ -108,6 +110,7 @@ cudaError_t launch_integrate_core(const int length[3], int L, const double *pol,
 
 // gpw_mixed.cu
 int mixed_build(TaskSet &ts, std::string &err);
+int mixed_rebin(TaskSet &ts, std::string &err);  // records and bins from ts.d_geom
 void mixed_free(TaskSet &ts);
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 cudaError_t launch_general_ff(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s);

@@ -149,6 +149,13 @@ struct MixedState {
     int sms = 0;
     int per_sm = 0, per_sm_i = 0, per_sm_ig = 0;  // resident CTAs: collocate, integrate (ortho, general)
     uint4 *d_vslot = nullptr;  // orthorhombic integrate: per-CTA V slots
+    // binning state kept for re-binning on the device (gpw_taskset_update_geometry)
+    std::vector<TileDesc> h_tiles;  // every tile of the binned levels, in tile-index order
+    struct BinLevel *d_bl = nullptr;  // per level: first tile index, tiles per axis, tile shape
+    int *d_blob_len = nullptr;      // per binned pair: chunks of its blob
+    int *d_count = nullptr;         // per tile: items
+    unsigned long long *d_cursor = nullptr;  // per tile: next item slot (fill pass)
+    int64_t cap_items = 0, cap_units = 0;    // capacities of d_items / d_iimg and d_tiles / d_start
 };
 
 
@@ -1442,47 +1449,174 @@ __global__ void k_item_images(const TileDesc *__restrict__ tiles, const int64_t 
     }
 }
 
-// scatters the records (contiguous on input) to their blob offsets
-__global__ void k_place_records(const uint4 *__restrict__ rec, const int64_t *__restrict__ off16, uint4 *blob,
-                                int64_t ntask) {
-    const int64_t n = ntask * kHdr16;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t k = i / kHdr16;
-        blob[off16[k] + (i - k * kHdr16)] = rec[i];
+// ---------------------------------------------------------------------------
+// Binning on the device: the (tile, pair) items of every binned pair.
+struct BinLevel {
+    int first;          // index of the level's first tile
+    int nt[3];          // tiles per axis
+    int lz;             // log2 of the tile z extent
+};
+
+// One axis of a pair's cube (cube offsets lb..hi around cc, as grid_base_ref_c.cc:318-351
+// maps them) cut into runs of consecutive grid indices inside one tile.
+struct AxisRuns {
+    int lb, hi, cc, T, N, npts, periodic, lbg;
+    bool dedupe;  // the cube spans so much of a periodic axis that two runs may hit one tile
+    __device__ void init(const LevelDev &lv, int d, int cc_, int lb_, int hi_, int T_) {
+        lb = lb_; hi = hi_; cc = cc_; T = T_;
+        N = lv.ngrid[d]; npts = lv.npts[d]; periodic = lv.periodic[d]; lbg = lv.lb_grid[d];
+        dedupe = periodic && (hi - lb + 1) + T > N;
+    }
+    // the run starting at offset gg: its tile and the smallest folded offset |f|
+    // (f = g <= 0 ? -g : g - 1) over it; gg moves past the run; false: outside the window
+    __device__ bool next(int &gg, int &t, int &f) const {
+        const int w = periodic ? imod(cc + gg, npts) : gg + imod(cc + lb + lbg, npts) - lb;
+        if (w < 0 || w >= N) {
+            gg++;
+            return false;
+        }
+        t = w / T;
+        const int len = min(T - (w - t * T), N - w);
+        const int g1 = min(gg + len - 1, hi);
+        f = (gg <= 1 && g1 >= 0) ? 0 : (g1 < 0 ? -g1 : gg - 1);
+        gg += len;
+        return true;
+    }
+    // calls fn(tile, fmin) once per tile the axis touches
+    template <class Fn>
+    __device__ void each(Fn &&fn) const {
+        for (int gg = lb; gg <= hi;) {
+            const int g0 = gg;
+            int t, f;
+            if (!next(gg, t, f)) continue;
+            if (dedupe) {  // only the first run into a tile reports it, with the minimum over all runs
+                bool seen = false;
+                for (int g2 = lb; g2 < g0 && !seen;) {
+                    int t2, f2;
+                    if (next(g2, t2, f2) && t2 == t) seen = true;
+                }
+                if (seen) continue;
+                for (int g2 = gg; g2 <= hi;) {
+                    int t2, f2;
+                    if (next(g2, t2, f2) && t2 == t) f = min(f, f2);
+                }
+            }
+            fn(t, f);
+        }
+    }
+};
+
+// Pass 0: items per tile (count).  Pass 1: item words into the tile's slots
+// (cursor).  A pair visits a tile only if some cube point of the tile can be
+// inside its sphere: folded distance of the tile's nearest offsets <= radius
+// (with a margin); explicit cube lists and general-cell boxes are not culled.
+__global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, const LevelDev *__restrict__ levels,
+                            const BinLevel *__restrict__ bl, const int64_t *__restrict__ off16,
+                            const int *__restrict__ len16, int pass, int *count, unsigned long long *cursor,
+                            uint64_t *items) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nbin; k += (int64_t)gridDim.x * blockDim.x) {
+        const PairGeom &g = geoms[k];
+        const LevelDev &lv = levels[g.level];
+        const BinLevel B = bl[g.level];
+        const TileShape sh(B.lz);
+        int lb[3], hi[3];
+        for (int d = 0; d < 3; d++) {  // general cell: the index box as a box-relative cube [0, hi - cc]
+            lb[d] = g.ortho ? g.lb[d] : 0;
+            hi[d] = g.ortho ? g.hi[d] : g.hi[d] - g.cc[d];
+        }
+        AxisRuns ax, ay, az;
+        ax.init(lv, 0, g.cc[0], lb[0], hi[0], TX);
+        ay.init(lv, 1, g.cc[1], lb[1], hi[1], sh.TY);
+        az.init(lv, 2, g.cc[2], lb[2], hi[2], sh.TZ);
+        const double r2 = g.radius * g.radius * (1.0 + 1e-9) + 1e-12;
+        const double hx = lv.dh[0][0], hy = lv.dh[1][1], hz = lv.dh[2][2];
+        const bool table = g.table_off >= 0 || !g.ortho;
+        const uint64_t word = ((uint64_t)off16[k] << 16) | (uint64_t)len16[k];
+        az.each([&](int tz, int fz) {
+            const double dz = fz * hz;
+            if (!table && dz * dz > r2) return;
+            ay.each([&](int ty, int fy) {
+                const double dy = fy * hy;
+                if (!table && dz * dz + dy * dy > r2) return;
+                ax.each([&](int tx, int fx) {
+                    const double dx = fx * hx;
+                    if (!table && dz * dz + dy * dy + dx * dx > r2) return;
+                    const int tile = B.first + (tz * B.nt[1] + ty) * B.nt[0] + tx;
+                    if (pass == 0) atomicAdd(count + tile, 1);
+                    else items[atomicAdd(cursor + tile, 1ull)] = word;
+                });
+            });
+        });
     }
 }
 
-// ---------------------------------------------------------------------------
-// host: bin the orthorhombic pairs by tile
-namespace {
-// Tiles one cube axis touches, with the smallest folded offset |f| (f = g <= 0 ?
-// -g : g - 1) of the cube offsets g that land in each tile.
-struct AxisTile {
-    int tile;
-    int fmin;
-};
-void axis_tiles(const LevelDev &lv, int d, const PairGeom &g, int T, std::vector<AxisTile> &out) {
-    out.clear();
-    const int N = lv.ngrid[d];
-    const int nt = (N + T - 1) / T;
-    std::vector<int> best(nt, INT32_MAX);
-    for (int gg = g.lb[d]; gg <= g.hi[d];) {
-        int w;
-        if (lv.periodic[d]) w = imod(g.cc[d] + gg, lv.npts[d]);
-        else w = gg + imod(g.cc[d] + g.lb[d] + lv.lb_grid[d], lv.npts[d]) - g.lb[d];
-        if (w < 0 || w >= N) { gg++; continue; }
-        const int t = w / T;
-        const int len = std::min(T - (w - t * T), N - w);
-        const int g1 = std::min(gg + len - 1, g.hi[d]);
-        // smallest folded offset over [gg, g1]
-        const int f = (gg <= 1 && g1 >= 0) ? 0 : (g1 < 0 ? -g1 : gg - 1);
-        best[t] = std::min(best[t], f);
-        gg += len;
+// The record (TPair) of every binned pair from its geometry, into its blob.
+__global__ void k_make_records(const PairGeom *__restrict__ geoms, int64_t nbin, const LevelDev *__restrict__ levels,
+                               const int64_t *__restrict__ off16, uint4 *blob) {
+    auto split = [](double d) {
+        const float h = __double2float_rn(d);
+        return ff{h, __double2float_rn(d - (double)h)};
+    };
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nbin; k += (int64_t)gridDim.x * blockDim.x) {
+        const PairGeom &g = geoms[k];
+        const LevelDev &lv = levels[g.level];
+        TPair p;
+        memset(&p, 0, sizeof p);
+        p.r2 = rmul(g.radius, g.radius);
+        p.r2f = __double2float_rn(p.r2);
+        p.zetp = split(g.zetp);
+        p.lp = g.lp;
+        p.L = g.lp + 1;
+        p.coef_off = g.coef_off;
+        if (!g.ortho) {
+            // general cell: t_d = (index_d - gp_d) |v_d|, the box as a cube [0, hi - cc] at cc
+            p.general = 1;
+            double len[3];
+            for (int d = 0; d < 3; d++)
+                len[d] = rsqrt_rn(radd(radd(rmul(lv.dh[d][0], lv.dh[d][0]), rmul(lv.dh[d][1], lv.dh[d][1])),
+                                       rmul(lv.dh[d][2], lv.dh[d][2])));
+            p.hx = rdiv(1.0, len[0]);
+            p.hy = rdiv(1.0, len[1]);
+            p.hz = rdiv(1.0, len[2]);
+            p.radius = g.radius;
+            for (int d = 0; d < 3; d++) {
+                p.h[d] = split(len[d]);
+                p.off[d] = split(rmul(rsub(g.off[d], (double)g.cc[d]), len[d]));
+                p.lb[d] = 0;
+                p.hi[d] = g.hi[d] - g.cc[d];
+                p.cc[d] = g.cc[d];
+                p.gp[d] = g.off[d];
+            }
+            p.table_off = -1;
+        } else {
+            p.hx = lv.dh[0][0];
+            p.hy = lv.dh[1][1];
+            p.hz = lv.dh[2][2];
+            p.hxf = __double2float_rn(p.hx);
+            p.hyf = __double2float_rn(p.hy);
+            p.hzf = __double2float_rn(p.hz);
+            p.hyinvf = __double2float_rn(rdiv(1.0, p.hy));
+            p.hxinvf = __double2float_rn(rdiv(1.0, p.hx));
+            for (int d = 0; d < 3; d++) {
+                p.off[d] = split(g.off[d]);
+                p.h[d] = split(lv.dh[d][d]);
+                p.lb[d] = g.lb[d];
+                p.hi[d] = g.hi[d];
+                p.cc[d] = g.cc[d];
+            }
+            p.kgmin = g.kgmin;
+            p.table_off = g.table_off;
+        }
+        const uint4 *src = reinterpret_cast<const uint4 *>(&p);
+        uint4 *dst = blob + off16[k];
+        for (int c = 0; c < (int)(sizeof(TPair) / 16); c++) dst[c] = src[c];
+        if (sizeof(TPair) % 16) {  // the record's last partial chunk
+            uint4 last = make_uint4(0, 0, 0, 0);
+            memcpy(&last, reinterpret_cast<const char *>(&p) + (sizeof(TPair) / 16) * 16, sizeof(TPair) % 16);
+            dst[sizeof(TPair) / 16] = last;
+        }
     }
-    for (int t = 0; t < nt; t++)
-        if (best[t] != INT32_MAX) out.push_back(AxisTile{t, best[t]});
 }
-}  // namespace
 
 int mixed_build(TaskSet &ts, std::string &err) {
     MixedState *M = new MixedState();
@@ -1563,80 +1697,16 @@ int mixed_build(TaskSet &ts, std::string &err) {
             for (int b = 0; b < nty[l]; b++)
                 for (int c = 0; c < ntx[l]; c++) tiles.push_back(TileDesc{l, {c, b, a}, ts.tile_lz[l], 0});
     }
-    int nto = 0;
-    while (nto < (int)tiles.size() && P.lv[tiles[nto].level].ortho) nto++;
-    M->ntiles_ortho = nto;
-    const int ntiles = (int)tiles.size();
-    std::vector<int64_t> count(ntiles + 1, 0);
-    std::vector<AxisTile> ax, ay, az;
-    // a pair visits a tile only if some cube point of the tile can be inside its
-    // sphere: folded distance of the tile's nearest offsets <= radius (with margin)
-    auto each = [&](auto &&fn) {
-        for (int64_t k = 0; k < nbin; k++) {
-            PairGeom g = ts.h_geom[k];
-            const LevelDev &lv = P.lv[g.level];
-            if (!g.ortho) {  // the index box as a box-relative cube: offsets [0, hi - cc]
-                for (int d = 0; d < 3; d++) {
-                    g.hi[d] -= g.cc[d];
-                    g.lb[d] = 0;
-                }
-            }
-            axis_tiles(lv, 0, g, TX, ax);
-            const TileShape sh(ts.tile_lz[g.level]);
-            axis_tiles(lv, 1, g, sh.TY, ay);
-            axis_tiles(lv, 2, g, sh.TZ, az);
-            const int base = lvl_first[g.level];
-            const double r2 = g.radius * g.radius * (1.0 + 1e-9) + 1e-12;
-            const double hx = lv.dh[0][0], hy = lv.dh[1][1], hz = lv.dh[2][2];
-            const bool table = g.table_off >= 0 || !g.ortho;  // cube lists, general boxes: no culling
-            for (const AxisTile &c : az) {
-                const double dz = c.fmin * hz;
-                if (!table && dz * dz > r2) continue;
-                for (const AxisTile &b : ay) {
-                    const double dy = b.fmin * hy;
-                    if (!table && dz * dz + dy * dy > r2) continue;
-                    for (const AxisTile &a : ax) {
-                        const double dx = a.fmin * hx;
-                        if (!table && dz * dz + dy * dy + dx * dx > r2) continue;
-                        fn(base + (c.tile * nty[g.level] + b.tile) * ntx[g.level] + a.tile, (int)k);
-                    }
-                }
-            }
-        }
-    };
-    each([&](int t, int) { count[t + 1]++; });
-    // items grouped by tile
-    std::vector<int64_t> start(ntiles + 1, 0);
-    for (int i = 0; i < ntiles; i++) start[i + 1] = start[i] + count[i + 1];
-    const int64_t nitems = start[ntiles];
-    // Work units for the persistent queue: a tile with more items than ~1/4 of
-    // an even share per resident CTA is divided into units of consecutive items
-    // (their flushes add with FP64 atomics); units ordered by decreasing work
-    // within each group (orthorhombic, general).
-    int sms_dev = 0;
-    cudaDeviceGetAttribute(&sms_dev, cudaDevAttrMultiProcessorCount, P.device);
-    const int64_t target = std::max<int64_t>(64, (nitems + 64LL * sms_dev - 1) / std::max(1, 64 * sms_dev));
-    struct Unit {
-        int tile;
-        int64_t it0, it1;
-        bool split;
-    };
-    std::vector<Unit> units;
-    for (int t = 0; t < ntiles; t++) {
-        const int64_t n = count[t + 1];
-        if (n == 0) continue;
-        const int64_t nu = (n + target - 1) / target;
-        for (int64_t u = 0; u < nu; u++)
-            units.push_back(Unit{t, start[t] + n * u / nu, start[t] + n * (u + 1) / nu, nu > 1});
+    M->h_tiles = tiles;
+    std::vector<BinLevel> blv(P.nlevels);
+    for (int l = 0; l < P.nlevels; l++) {
+        blv[l].first = lvl_first[l];
+        blv[l].nt[0] = lvl_first[l] >= 0 ? ntx[l] : 0;
+        blv[l].nt[1] = lvl_first[l] >= 0 ? nty[l] : 0;
+        blv[l].nt[2] = lvl_first[l] >= 0 ? ntz[l] : 0;
+        blv[l].lz = ts.tile_lz[l] >= 0 ? ts.tile_lz[l] : kDefaultTileLz;
     }
-    std::stable_sort(units.begin(), units.end(), [&](const Unit &a, const Unit &b) {
-        const bool ga = a.tile >= nto, gb = b.tile >= nto;
-        if (ga != gb) return !ga;
-        return a.it1 - a.it0 > b.it1 - b.it0;
-    });
-    const int nunits = (int)units.size();
-    int nuo = 0;
-    while (nuo < nunits && units[nuo].tile < nto) nuo++;
+    const int ntiles = (int)tiles.size();
     // blob layout: per task the record, then its coefficients
     std::vector<int64_t> off16((size_t)std::max<int64_t>(nbin, 1), 0);
     std::vector<int> len16((size_t)std::max<int64_t>(nbin, 1), 0);
@@ -1646,125 +1716,27 @@ int mixed_build(TaskSet &ts, std::string &err) {
         len16[k] = kHdr16 + (ncoef(ts.h_geom[k].lp) * (int)sizeof(float2) + 15) / 16;
         nchunks += len16[k];
     }
-    std::vector<uint64_t> items((size_t)std::max<int64_t>(nitems, 1));
-    std::vector<int64_t> fill(start.begin(), start.end() - 1);
-    each([&](int t, int k) { items[fill[t]++] = ((uint64_t)off16[k] << 16) | (uint64_t)len16[k]; });
-    std::vector<TileDesc> tiles_sorted(std::max(nunits, 1));
-    std::vector<int64_t> ubounds(2 * (size_t)std::max(nunits, 1), 0);  // per unit: first item, end
-    for (int u = 0; u < nunits; u++) {
-        tiles_sorted[u] = tiles[units[u].tile];
-        tiles_sorted[u].split = units[u].split ? 1 : 0;
-        ubounds[2 * u] = units[u].it0;
-        ubounds[2 * u + 1] = units[u].it1;
-    }
-    M->ntiles_ortho = nuo;
-    M->ntiles = nunits;
-    M->nitems = nitems;
     cudaError_t e = cudaSuccess;
     auto alloc = [&](void **p, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 16));
     };
-    std::vector<uint4> recs((size_t)std::max<int64_t>(nbin, 1) * kHdr16);
-    auto split = [](double d) {
-        const float h = (float)d;
-        return ff{h, (float)(d - (double)h)};
-    };
-    for (int64_t k = 0; k < nbin; k++) {
-        const PairGeom &g = ts.h_geom[k];
-        const LevelDev &lv = P.lv[g.level];
-        TPair p;
-        memset(&p, 0, sizeof p);
-        if (!g.ortho) {
-            // general cell: t_d = (index_d - gp_d) |v_d|, the box as a cube [0, hi - cc] at cc
-            p.general = 1;
-            p.r2 = rmul(g.radius, g.radius);
-            p.hx = 1.0 / std::sqrt(lv.dh[0][0] * lv.dh[0][0] + lv.dh[0][1] * lv.dh[0][1] + lv.dh[0][2] * lv.dh[0][2]);
-            p.hy = 1.0 / std::sqrt(lv.dh[1][0] * lv.dh[1][0] + lv.dh[1][1] * lv.dh[1][1] + lv.dh[1][2] * lv.dh[1][2]);
-            p.hz = 1.0 / std::sqrt(lv.dh[2][0] * lv.dh[2][0] + lv.dh[2][1] * lv.dh[2][1] + lv.dh[2][2] * lv.dh[2][2]);
-            p.r2f = (float)p.r2;
-            p.radius = g.radius;
-            p.zetp = split(g.zetp);
-            for (int d = 0; d < 3; d++) {
-                const double hd = std::sqrt(lv.dh[d][0] * lv.dh[d][0] + lv.dh[d][1] * lv.dh[d][1] +
-                                            lv.dh[d][2] * lv.dh[d][2]);
-                p.h[d] = split(hd);
-                p.off[d] = split((g.off[d] - (double)g.cc[d]) * hd);
-                p.lb[d] = 0;
-                p.hi[d] = g.hi[d] - g.cc[d];
-                p.cc[d] = g.cc[d];
-                p.gp[d] = g.off[d];
-            }
-            p.lp = g.lp;
-            p.L = g.lp + 1;
-            p.coef_off = g.coef_off;
-            p.table_off = -1;
-            memcpy(&recs[(size_t)k * kHdr16], &p, sizeof p);
-            continue;
-        }
-        p.r2 = rmul(g.radius, g.radius);
-        p.hx = lv.dh[0][0];
-        p.hy = lv.dh[1][1];
-        p.hz = lv.dh[2][2];
-        p.r2f = (float)p.r2;
-        p.hxf = (float)p.hx;
-        p.hyf = (float)p.hy;
-        p.hzf = (float)p.hz;
-        p.hyinvf = (float)(1.0 / p.hy);
-        p.hxinvf = (float)(1.0 / p.hx);
-        p.zetp = split(g.zetp);
-        for (int d = 0; d < 3; d++) {
-            p.off[d] = split(g.off[d]);
-            p.h[d] = split(lv.dh[d][d]);
-            p.lb[d] = g.lb[d];
-            p.hi[d] = g.hi[d];
-            p.cc[d] = g.cc[d];
-        }
-        p.kgmin = g.kgmin;
-        p.lp = g.lp;
-        p.L = g.lp + 1;
-        p.coef_off = g.coef_off;
-        p.table_off = g.table_off;
-        memcpy(&recs[(size_t)k * kHdr16], &p, sizeof p);
-    }
     alloc((void **)&M->d_blob, sizeof(uint4) * (size_t)std::max<int64_t>(nchunks, 1));
     alloc((void **)&M->d_blob_off, sizeof(int64_t) * off16.size());
+    alloc((void **)&M->d_blob_len, sizeof(int) * len16.size());
+    alloc((void **)&M->d_bl, sizeof(BinLevel) * blv.size());
+    alloc((void **)&M->d_count, sizeof(int) * (size_t)std::max(ntiles, 1));
+    alloc((void **)&M->d_cursor, sizeof(unsigned long long) * (size_t)std::max(ntiles, 1));
+    alloc((void **)&M->d_queue, sizeof(int) * 5);  // [4]: status sink of the set-up kernels
+    alloc((void **)&M->d_glv, sizeof(GenLevel) * glv.size());
     if (e == cudaSuccess) e = cudaMemset(M->d_blob, 0, sizeof(uint4) * (size_t)std::max<int64_t>(nchunks, 1));
     if (e == cudaSuccess)
         e = cudaMemcpy(M->d_blob_off, off16.data(), sizeof(int64_t) * off16.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && nbin > 0) {
-        uint4 *d_recs = nullptr;
-        e = cudaMalloc(&d_recs, sizeof(uint4) * recs.size());
-        if (e == cudaSuccess) e = cudaMemcpy(d_recs, recs.data(), sizeof(uint4) * recs.size(), cudaMemcpyHostToDevice);
-        if (e == cudaSuccess) {
-            k_place_records<<<(unsigned)std::min<int64_t>((nbin * kHdr16 + 255) / 256, 8192), 256>>>(
-                d_recs, M->d_blob_off, M->d_blob, nbin);
-            e = cudaGetLastError();
-        }
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
-        cudaFree(d_recs);
-    }
-    alloc((void **)&M->d_tiles, sizeof(TileDesc) * tiles_sorted.size());
-    alloc((void **)&M->d_start, sizeof(int64_t) * ubounds.size());
-    alloc((void **)&M->d_items, sizeof(uint64_t) * items.size());
-    alloc((void **)&M->d_iimg, sizeof(ItemImg) * items.size());
-    alloc((void **)&M->d_queue, sizeof(int) * 5);  // [4]: status sink of the set-up kernels
-    alloc((void **)&M->d_glv, sizeof(GenLevel) * glv.size());
+    if (e == cudaSuccess)
+        e = cudaMemcpy(M->d_blob_len, len16.data(), sizeof(int) * len16.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(M->d_bl, blv.data(), sizeof(BinLevel) * blv.size(), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(M->d_glv, glv.data(), sizeof(GenLevel) * glv.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && nunits)
-        e = cudaMemcpy(M->d_tiles, tiles_sorted.data(), sizeof(TileDesc) * nunits, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(M->d_start, ubounds.data(), sizeof(int64_t) * ubounds.size(), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && nitems)
-        e = cudaMemcpy(M->d_items, items.data(), sizeof(uint64_t) * nitems, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess && nitems) {
-        // image overflows are reported by the tiled kernels when they run (a plain
-        // FP64 call on this task set must not see them)
-        k_item_images<<<std::max(1, std::min(nunits, 8192)), 128>>>(M->d_tiles, M->d_start, M->d_items, M->d_blob,
-                                                                    P.d_levels, M->d_iimg, nunits, M->d_queue + 4);
-        e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    }
+    if (e == cudaSuccess) e = cudaMemset(M->d_queue, 0, sizeof(int) * 5);
     if (e != cudaSuccess) {
         err = std::string("mixed_build: ") + cudaGetErrorString(e);
         return GPW_ERR_CUDA;
@@ -1800,17 +1772,135 @@ int mixed_build(TaskSet &ts, std::string &err) {
     M->per_sm = per_sm;
     M->per_sm_i = per_sm_i;
     M->per_sm_ig = resident(ki[1], sizeof(SmemInt<true>));
+    M->sms = sms;
     // one V slot per resident orthorhombic integrate CTA
-    if (M->ntiles_ortho > 0) {
+    if (northo > 0) {
         e = cudaMalloc(&M->d_vslot, sizeof(uint4) * kVSlot16 * (size_t)sms * per_sm_i);
         if (e != cudaSuccess) {
             err = std::string("mixed_build: ") + cudaGetErrorString(e);
             return GPW_ERR_CUDA;
         }
     }
-    M->grid_ctas_i = std::max(1, std::min(nunits, sms * per_sm_i));
-    M->grid_ctas = std::max(1, std::min(nunits, sms * per_sm));
-    M->sms = sms;
+    return mixed_rebin(ts, err);
+}
+
+// Records, items, work units and item images from the task set's current device
+// geometry (ts.d_geom): at creation and after a geometry update.  The tile
+// grid, the blob layout and the choice of kernels stay as mixed_build made them.
+int mixed_rebin(TaskSet &ts, std::string &err) {
+    MixedState *M = ts.mixed;
+    const Plan &P = *ts.plan;
+    const int64_t nbin = M->nbin;
+    const int ntiles = (int)M->h_tiles.size();
+    cudaError_t e = cudaSuccess;
+    auto fail = [&](cudaError_t ce) {
+        err = std::string("mixed_rebin: ") + cudaGetErrorString(ce);
+        return GPW_ERR_CUDA;
+    };
+    const unsigned nblk = (unsigned)std::max<int64_t>(1, std::min<int64_t>((nbin + 127) / 128, 8192));
+    if (nbin > 0) {
+        k_make_records<<<nblk, 128>>>(ts.d_geom, nbin, P.d_levels, M->d_blob_off, M->d_blob);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+    }
+    if ((e = cudaMemset(M->d_count, 0, sizeof(int) * (size_t)std::max(ntiles, 1))) != cudaSuccess) return fail(e);
+    if (nbin > 0) {
+        k_bin_pairs<<<nblk, 128>>>(ts.d_geom, nbin, P.d_levels, M->d_bl, M->d_blob_off, M->d_blob_len, 0,
+                                   M->d_count, nullptr, nullptr);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+    }
+    std::vector<int> count((size_t)std::max(ntiles, 1), 0);
+    if ((e = cudaMemcpy(count.data(), M->d_count, sizeof(int) * count.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return fail(e);
+    // items grouped by tile
+    std::vector<int64_t> start(ntiles + 1, 0);
+    for (int i = 0; i < ntiles; i++) start[i + 1] = start[i] + count[i];
+    const int64_t nitems = start[ntiles];
+    int nto = 0;
+    while (nto < ntiles && P.lv[M->h_tiles[nto].level].ortho) nto++;
+    // Work units for the persistent queue: a tile with more items than ~1/64 of
+    // an even share per SM is divided into units of consecutive items (their
+    // flushes add with FP64 atomics); units ordered by decreasing work within
+    // each group (orthorhombic, general).
+    const int64_t target = std::max<int64_t>(64, (nitems + 64LL * M->sms - 1) / std::max(1, 64 * M->sms));
+    struct Unit {
+        int tile;
+        int64_t it0, it1;
+        bool split;
+    };
+    std::vector<Unit> units;
+    for (int t = 0; t < ntiles; t++) {
+        const int64_t n = count[t];
+        if (n == 0) continue;
+        const int64_t nu = (n + target - 1) / target;
+        for (int64_t u = 0; u < nu; u++)
+            units.push_back(Unit{t, start[t] + n * u / nu, start[t] + n * (u + 1) / nu, nu > 1});
+    }
+    std::stable_sort(units.begin(), units.end(), [&](const Unit &a, const Unit &b) {
+        const bool ga = a.tile >= nto, gb = b.tile >= nto;
+        if (ga != gb) return !ga;
+        return a.it1 - a.it0 > b.it1 - b.it0;
+    });
+    const int nunits = (int)units.size();
+    int nuo = 0;
+    while (nuo < nunits && units[nuo].tile < nto) nuo++;
+    std::vector<TileDesc> tiles_sorted(std::max(nunits, 1));
+    std::vector<int64_t> ubounds(2 * (size_t)std::max(nunits, 1), 0);  // per unit: first item, end
+    for (int u = 0; u < nunits; u++) {
+        tiles_sorted[u] = M->h_tiles[units[u].tile];
+        tiles_sorted[u].split = units[u].split ? 1 : 0;
+        ubounds[2 * u] = units[u].it0;
+        ubounds[2 * u + 1] = units[u].it1;
+    }
+    // storage for the items and units (kept when large enough)
+    if (nitems > M->cap_items || !M->d_items) {
+        cudaFree(M->d_items);
+        cudaFree(M->d_iimg);
+        M->d_items = nullptr;
+        M->d_iimg = nullptr;
+        const int64_t cap = std::max<int64_t>(nitems + nitems / 16, 1);
+        if ((e = cudaMalloc(&M->d_items, sizeof(uint64_t) * cap)) != cudaSuccess) return fail(e);
+        if ((e = cudaMalloc(&M->d_iimg, sizeof(ItemImg) * cap)) != cudaSuccess) return fail(e);
+        M->cap_items = cap;
+    }
+    if (nunits > M->cap_units || !M->d_tiles) {
+        cudaFree(M->d_tiles);
+        cudaFree(M->d_start);
+        M->d_tiles = nullptr;
+        M->d_start = nullptr;
+        const int64_t cap = std::max<int64_t>(nunits + nunits / 16, 1);
+        if ((e = cudaMalloc(&M->d_tiles, sizeof(TileDesc) * cap)) != cudaSuccess) return fail(e);
+        if ((e = cudaMalloc(&M->d_start, sizeof(int64_t) * 2 * cap)) != cudaSuccess) return fail(e);
+        M->cap_units = cap;
+    }
+    if (nunits && (e = cudaMemcpy(M->d_tiles, tiles_sorted.data(), sizeof(TileDesc) * nunits,
+                                  cudaMemcpyHostToDevice)) != cudaSuccess)
+        return fail(e);
+    if ((e = cudaMemcpy(M->d_start, ubounds.data(), sizeof(int64_t) * ubounds.size(), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+        return fail(e);
+    std::vector<unsigned long long> cur((size_t)std::max(ntiles, 1), 0ull);
+    for (int t = 0; t < ntiles; t++) cur[t] = (unsigned long long)start[t];
+    if ((e = cudaMemcpy(M->d_cursor, cur.data(), sizeof(unsigned long long) * cur.size(), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+        return fail(e);
+    if (nbin > 0) {
+        k_bin_pairs<<<nblk, 128>>>(ts.d_geom, nbin, P.d_levels, M->d_bl, M->d_blob_off, M->d_blob_len, 1,
+                                   nullptr, M->d_cursor, M->d_items);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+    }
+    if (nitems) {
+        // image overflows are reported by the tiled kernels when they run (a plain
+        // FP64 call on this task set must not see them)
+        k_item_images<<<std::max(1, std::min(nunits, 8192)), 128>>>(M->d_tiles, M->d_start, M->d_items, M->d_blob,
+                                                                    P.d_levels, M->d_iimg, nunits, M->d_queue + 4);
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+    }
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e);
+    M->ntiles_ortho = nuo;
+    M->ntiles = nunits;
+    M->nitems = nitems;
+    M->grid_ctas_i = std::max(1, std::min(nunits, M->sms * M->per_sm_i));
+    M->grid_ctas = std::max(1, std::min(nunits, M->sms * M->per_sm));
     return GPW_SUCCESS;
 }
 
@@ -1826,6 +1916,10 @@ void mixed_free(TaskSet &ts) {
     cudaFree(M->d_queue);
     cudaFree(M->d_glv);
     cudaFree(M->d_vslot);
+    cudaFree(M->d_bl);
+    cudaFree(M->d_blob_len);
+    cudaFree(M->d_count);
+    cudaFree(M->d_cursor);
     delete M;
     ts.mixed = nullptr;
 }

@@ -1,28 +1,33 @@
 """Test-harness-only torch.autograd.Function over the C ABI: the energy
 E = sum_levels <V, rho(pab, ra, rb, zeta, zetb)> with the library's forward
-(gpw_collocate) and backward (gpw_backward) kernels."""
-import numpy as np
+(gpw_collocate) and backward (gpw_backward) kernels.  One task set serves every
+evaluation: each forward moves its pairs with gpw_taskset_update_geometry (on the
+device) instead of rebuilding it on the host."""
 import torch
 
 from libgpw_gb300 import capi, tasks as T
 
 
+class PairSet:
+    """The task set of a workload, created once and moved by every forward."""
+
+    def __init__(self, wl):
+        self.wl = wl
+        self.plan = capi.Plan(wl.levels)
+        self.ts = capi.TaskSet.from_workload(self.plan, wl)
+
+
 class Energy(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, pab, ra, rb, zeta, zetb, V, template):
-        wl = template
-        t = wl.tasks.copy()
-        t["ra"] = ra.detach().cpu().numpy()
-        t["rab"] = (rb - ra).detach().cpu().numpy()
-        t["zeta"] = zeta.detach().cpu().numpy()
-        t["zetb"] = zetb.detach().cpu().numpy()
-        plan = capi.Plan(wl.levels)
-        ts = capi.TaskSet(plan, t, wl.compute_tau)
+    def forward(ctx, pab, ra, rb, zeta, zetb, V, pairs):
+        ts, wl = pairs.ts, pairs.wl
+        ts.update_geometry(ra.detach().contiguous(), (rb - ra).detach().contiguous(), zeta.detach().contiguous(),
+                           zetb.detach().contiguous())
         dev = pab.device
         grids = [torch.zeros(T.grid_shape(g), dtype=torch.float64, device=dev) for g in wl.levels]
         ts.collocate(pab.detach().contiguous(), grids, "fp64")
         E = sum((g * v).sum() for g, v in zip(grids, V))
-        ctx.ts, ctx.plan, ctx.V = ts, plan, V
+        ctx.ts, ctx.V = ts, V
         ctx.save_for_backward(pab)
         return E
 
@@ -41,5 +46,5 @@ class Energy(torch.autograd.Function):
         return gE * hab, gE * dra, gE * drb, gE * dza, gE * dzb, None, None
 
 
-def energy(pab, ra, rb, zeta, zetb, V, template):
-    return Energy.apply(pab, ra, rb, zeta, zetb, V, template)
+def energy(pab, ra, rb, zeta, zetb, V, pairs):
+    return Energy.apply(pab, ra, rb, zeta, zetb, V, pairs)

@@ -145,7 +145,7 @@ def test_autograd_function(oracle_lib):
     to the density blocks, centres and exponents through gpw_backward."""
     import torch
 
-    from gpw_autograd import energy
+    from gpw_autograd import PairSet, energy
 
     wl = workload(True, n=6, seed=43)
     V = wl.potentials(seed=8)
@@ -156,14 +156,25 @@ def test_autograd_function(oracle_lib):
     za = torch.from_numpy(wl.tasks["zeta"].copy()).to(dev).requires_grad_(True)
     zb = torch.from_numpy(wl.tasks["zetb"].copy()).to(dev).requires_grad_(True)
     Vd = [torch.from_numpy(v).to(dev) for v in V]
-    E = energy(pab, ra, rb, za, zb, Vd, wl)
+    pairs = PairSet(wl)
+    E = energy(pab, ra, rb, za, zb, Vd, pairs)
     gp, gra, grb, gza, gzb = torch.autograd.grad(E, [pab, ra, rb, za, zb])
     # dE/dpab is the oracle's integrate; E itself is the oracle's <V, rho>
     hab = oracle_lib.batch(wl, V=V)
     assert np.abs(gp.cpu().numpy() - hab).max() <= 1e-12 * np.abs(hab).max()
     E_cpu = sum(float(np.sum(g * v)) for g, v in zip(oracle_lib.batch(wl), V))
-    assert abs(float(E) - E_cpu) <= 1e-12 * max(abs(E_cpu), 1.0)
+    assert abs(float(E.detach()) - E_cpu) <= 1e-12 * max(abs(E_cpu), 1.0)
     assert torch.all(torch.isfinite(gra)) and torch.all(torch.isfinite(gza))
+    # a second evaluation at moved centres through the same task set (device update)
+    shift = torch.full_like(ra, 0.05)
+    ra2 = (ra.detach() + shift).requires_grad_(True)
+    rb2 = (rb.detach() + shift).requires_grad_(True)
+    E2 = energy(pab, ra2, rb2, za, zb, Vd, pairs)
+    t2 = wl.tasks.copy()
+    t2["ra"] = t2["ra"] + 0.05
+    w2 = T.Workload("moved", t2, wl.levels, wl.pab)
+    E2_cpu = sum(float(np.sum(g * v)) for g, v in zip(oracle_lib.batch(w2), V))
+    assert abs(float(E2.detach()) - E2_cpu) <= 1e-12 * max(abs(E2_cpu), 1.0)
 
 
 def test_backward_tau_high_l_general_cell_rejected():
