@@ -56,7 +56,7 @@ namespace gpw {
 
 constexpr int TX = 32;
 constexpr int MROWS = 128;       // TY * TZ rows per tile, one per thread
-constexpr int kMaxTY = 32, kMaxTZ = 16;
+constexpr int kMaxTY = 32, kMaxTZ = 8;  // tiles of 32 x 16 x 8 or 32 x 32 x 4
 constexpr int kMaxTZColl = 8;  // collocate keeps its stage-1 output for at most 8 z (tiles with TZ <= 8)
 constexpr int NTHR = MROWS;
 constexpr int NSL = 4;          // slices per operand
@@ -820,6 +820,73 @@ __device__ __forceinline__ int item_images(TileCommon &cm, const ItemImg &ii, co
 }
 
 
+// Stage 1 of collocate: Cxy[z][(b,a)] = sum_g c'[g][b][a] Z[g][z]; one output per
+// thread (16 consecutive threads share (b, a)), two partial sums over even and
+// odd g; the packed index of (g, b, a) is zs[g] - b g + k0.
+__device__ __forceinline__ void stage1_cxy(SmemColl &sm, int L, int lp, const TileShape &sh) {
+    const TileCommon &cm = sm.c;
+    const int npair = (L * (L + 1)) / 2;
+    const unsigned char *qbL = sm.qb[L - 1];
+    for (int t = threadIdx.x; t < sh.TZ * npair; t += NTHR) {
+        const int zz = t & (sh.TZ - 1), q = t >> sh.lz;
+        const int b = qbL[q];
+        const int a = q - (b * L - (b * (b - 1)) / 2), n = lp - a - b;
+        const int k0 = b * (lp + 1) - (b * (b - 1)) / 2 + a;
+        ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+        int g = 0, bg = 0;
+        for (; g + 1 <= n; g += 2, bg += 2 * b) {
+            s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
+            s1 = ff_fma(sm.rc[sm.zs[g + 1] - bg - b + k0], cm.Z[g + 1][zz], s1);
+        }
+        if (g <= n) s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
+        sm.Cxy[zz][q] = ff_add(s0, s1);
+    }
+}
+
+// Stage 2 of collocate for this thread's row (z, y), all a at once, then the
+// row's A slices (K slots below kw rewritten); returns the row exponent.  a in
+// pairs (a0, a0 + 1; unrolled, uniform exit at lp), b inner (runtime bound
+// lp - a0): only the products that exist, two independent float-float sums, each
+// renormalised once at the end.
+__device__ __forceinline__ int stage2_row(SmemColl &sm, const TileCommon &cm, int L, int lp, int sb, int z, int y,
+                                          bool live, int kw, int m) {
+    ff cx[kNPow];
+#pragma unroll
+    for (int a = 0; a < kNPow; a++) cx[a] = ff{0.0f, 0.0f};
+    float mx = 0.0f;
+    if (live) {
+        const ff *crow = sm.Cxy[z];
+#pragma unroll
+        for (int a0 = 0; a0 < kNPow; a0 += 2) {
+            if (a0 > lp) break;
+            ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+            const int nb = lp - a0;
+            int q = a0;  // pair_index(L, b, a0); (b, a0 + 1) is q + 1
+#pragma unroll 1
+            for (int b = 0; b <= nb; b++) {
+                const ff yb = cm.Y[b][y];
+                ff_acc_lazy(s0, crow[q], yb);
+                if (b < nb) ff_acc_lazy(s1, crow[q + 1], yb);  // a0 + 1 + b <= lp
+                q += L - b;
+            }
+            cx[a0] = fast_two_sum(s0.hi, s0.lo);
+            if (a0 + 1 < kNPow) cx[a0 + 1] = fast_two_sum(s1.hi, s1.lo);
+        }
+#pragma unroll
+        for (int a = 0; a < kNPow; a++) {
+            const float bal = pow2i(a * sb);  // balancing of the x powers (exact)
+            cx[a].hi = __fmul_rn(cx[a].hi, bal);
+            cx[a].lo = __fmul_rn(cx[a].lo, bal);
+            mx = fmaxf(mx, fabsf(cx[a].hi));  // entries a > lp are zero
+        }
+    }
+    const int em = exp_of(mx);
+    const float sc = em == kZeroExp ? 0.0f : pow2i(SLB - em);
+    // entries a > lp of cx are zero; K slots that may hold an earlier pair's values are rewritten
+    slice_row16(cx, sc, kw, L, sm.A[0], MROWS * KP, m);
+    return em;
+}
+
 // ---------------------------------------------------------------------------
 // kGeneral: tiles of general-cell levels.  The tables, stages and slices are the
 // same in t_d = (index_d - gp_d) |v_d|; the row ranges come from the quadratic
@@ -910,27 +977,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     recentre_x(pb, Q.tc, sm.rc, sm.bin, sm.zs, sm.qb, 64, NTHR - 64);
                 }
                 __syncthreads();
-                // stage 1: Cxy[z][(b,a)] = sum_g c'[g][b][a] Z[g][z]; one output per thread (16
-                // consecutive threads share (b, a)), two partial sums over even and odd g; the
-                // packed index of (g, b, a) is zs[g] - b g + k0
-                {
-                    const int npair = (L * (L + 1)) / 2;
-                    const unsigned char *qbL = sm.qb[L - 1];
-                    for (int t = tid; t < TZ * npair; t += NTHR) {
-                        const int zz = t & (TZ - 1), q = t >> sh.lz;
-                        const int b = qbL[q];
-                        const int a = q - (b * L - (b * (b - 1)) / 2), n = lp - a - b;
-                        const int k0 = b * (lp + 1) - (b * (b - 1)) / 2 + a;
-                        ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
-                        int g = 0, bg = 0;
-                        for (; g + 1 <= n; g += 2, bg += 2 * b) {
-                            s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
-                            s1 = ff_fma(sm.rc[sm.zs[g + 1] - bg - b + k0], cm.Z[g + 1][zz], s1);
-                        }
-                        if (g <= n) s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
-                        sm.Cxy[zz][q] = ff_add(s0, s1);
-                    }
-                }
+                stage1_cxy(sm, L, lp, sh);
                 __syncthreads();
                 // stage 2 (this thread's row, all a at once) + culling + A slices
                 int x0, x1;
@@ -939,47 +986,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                                       x1);
                 else
                     row_range(P, Q, A.table, Q.o[2] + z, Q.o[1] + y, z < ext_z && y < ext_y, x0, x1);
-                ff cx[kNPow];
-#pragma unroll
-                for (int a = 0; a < kNPow; a++) cx[a] = ff{0.0f, 0.0f};
-                float mx = 0.0f;
-                if (x0 <= x1) {
-                    // a in pairs (a0, a0 + 1; unrolled, uniform exit at lp), b inner (runtime
-                    // bound lp - a0): only the products that exist, two independent float-float
-                    // sums, each renormalised once at the end
-                    const ff *crow = sm.Cxy[z];
-#pragma unroll
-                    for (int a0 = 0; a0 < kNPow; a0 += 2) {
-                        if (a0 > lp) break;
-                        ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
-                        const int nb = lp - a0;
-                        int q = a0;  // pair_index(L, b, a0); (b, a0 + 1) is q + 1
-#pragma unroll 1
-                        for (int b = 0; b <= nb; b++) {
-                            const ff yb = cm.Y[b][y];
-                            ff_acc_lazy(s0, crow[q], yb);
-                            if (b < nb) ff_acc_lazy(s1, crow[q + 1], yb);  // a0 + 1 + b <= lp
-                            q += L - b;
-                        }
-                        cx[a0] = fast_two_sum(s0.hi, s0.lo);
-                        if (a0 + 1 < kNPow) cx[a0 + 1] = fast_two_sum(s1.hi, s1.lo);
-                    }
-                    const int sb = Q.sb;
-#pragma unroll
-                    for (int a = 0; a < kNPow; a++) {
-                        const float bal = pow2i(a * sb);  // balancing of the x powers (exact)
-                        cx[a].hi = __fmul_rn(cx[a].hi, bal);
-                        cx[a].lo = __fmul_rn(cx[a].lo, bal);
-                        mx = fmaxf(mx, fabsf(cx[a].hi));  // entries a > lp are zero
-                    }
-                }
-                const int em = exp_of(mx);
-                {
-                    const float sc = em == kZeroExp ? 0.0f : pow2i(SLB - em);
-                    // entries a > lp of cx are zero; K slots that may hold an earlier pair's
-                    // values (below kmax) are rewritten
-                    slice_row16(cx, sc, max(L, cm.kmax), L, sm.A[0], MROWS * KP, m);
-                }
+                const int em = stage2_row(sm, cm, L, lp, Q.sb, z, y, x0 <= x1, max(L, cm.kmax), m);
                 // stage 3 on the tensor cores: D_s = sum_{i+j=s} A_i B_j^T
                 tc::fence_async_smem();
                 tc::fence_before_sync();
