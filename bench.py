@@ -48,7 +48,40 @@ def parse():
     ap.add_argument("--no-graph", action="store_true", help="launch the step directly instead of replaying a CUDA graph")
     ap.add_argument("--no-tune", action="store_true",
                     help="tile shapes from the autotuner's table or the default, never timed here")
+    ap.add_argument("--dropin", type=int, default=0, metavar="CALLS",
+                    help="instead: time CALLS calls of the single-pair drop-in entry on each of the reference's "
+                         "task fixtures (host grid in and out, as the reference's replay calls it)")
     return ap.parse_args()
+
+
+def dropin_bench(calls: int) -> None:
+    """Microseconds per call of gpw_collocate_pgf_product_rspace (the drop-in for the
+    reference's grid_collocate_pgf_product_rspace) on the reference's four task
+    fixtures, against the CPU restatement of the same call (oracle, one thread)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from golden_io import TASK_NAMES, load_task
+    from libgpw_gb300 import capi
+    from oracle import oracle as O
+
+    out = {}
+    for name in TASK_NAMES:
+        d = load_task(name)
+        grid = np.zeros((int(d["ngrid"][2]), int(d["ngrid"][1]), int(d["ngrid"][0])))
+        for _ in range(20):
+            capi.collocate_pgf_product_rspace(d, grid)
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            capi.collocate_pgf_product_rspace(d, grid)
+        gpu_us = (time.perf_counter() - t0) / calls * 1e6
+        g2 = np.zeros_like(grid)
+        n_cpu = max(10, min(calls, 2000))
+        t0 = time.perf_counter()
+        for _ in range(n_cpu):
+            O.collocate(d, g2)
+        cpu_us = (time.perf_counter() - t0) / n_cpu * 1e6
+        out[name] = {"gpu_us_per_call": gpu_us, "cpu_oracle_us_per_call": cpu_us, "calls": calls,
+                     "grid": list(grid.shape)}
+    print(json.dumps({"metric": "drop-in single-pair collocate, us per call", "tasks": out}))
 
 
 # ----------------------------------------------------------------------------
@@ -248,6 +281,9 @@ def reference_arm(args):
 # ----------------------------------------------------------------------------
 def main():
     args = parse()
+    if args.dropin:
+        dropin_bench(args.dropin)
+        return
     if args.impl == "reference":
         reference_arm(args)
         return

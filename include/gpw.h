@@ -248,6 +248,16 @@ int gpw_taskset_autotune(gpw_taskset *ts, const double *d_pab, int *tile_z, doub
 int gpw_selftest_tensorcore(int64_t *mismatches);
 
 /*
+ * Self test of the float-float exponential of the mixed path (no reference
+ * counterpart): npoints arguments over [-60, 88) and npoints / 4 over [-103, -60),
+ * each a float-float value (a low part of up to half an ulp), against the FP64
+ * exp of the same value on the current device.  *max_rel_err receives the
+ * largest relative error where the result has a normal low part (a > -60),
+ * *max_rel_err_low the largest below (the low part underflows gradually there).
+ */
+int gpw_selftest_ff_exp(int64_t npoints, double *max_rel_err, double *max_rel_err_low);
+
+/*
  * Collocation that allocates no device memory (no counterpart in the
  * reference).  For callers that cannot allocate on their call path, because
  * their device memory belongs to their own pool allocator.  Collocates up to

@@ -70,6 +70,7 @@ def lib():
         "gpw_taskset_get_tiles": ([vp, vp], i32),
         "gpw_taskset_autotune": ([vp, vp, vp, vp, vp], i32),
         "gpw_selftest_tensorcore": ([C.POINTER(i64)], i32),
+        "gpw_selftest_ff_exp": ([i64, C.POINTER(dbl), C.POINTER(dbl)], i32),
         "gpw_collocate_noalloc": ([vp, vp, i32, i32, vp, vp, vp], i32),
         "gpw_collocate_core": ([vp, i32, vp, vp, i32, vp, vp], i32),
         "gpw_integrate_core": ([vp, i32, vp, i32, vp, vp, vp], i32),
@@ -258,6 +259,14 @@ def selftest_tensorcore() -> int:
     n = C.c_int64(-1)
     check(lib().gpw_selftest_tensorcore(C.byref(n)), "gpw_selftest_tensorcore")
     return n.value
+
+
+def selftest_ff_exp(npoints: int = 1 << 22) -> tuple:
+    """Runs gpw_selftest_ff_exp: (largest relative error where the result's low
+    part is normal, largest relative error below that)."""
+    a, b = C.c_double(-1.0), C.c_double(-1.0)
+    check(lib().gpw_selftest_ff_exp(int(npoints), C.byref(a), C.byref(b)), "gpw_selftest_ff_exp")
+    return a.value, b.value
 
 
 def collocate_pgf_product_rspace(t: dict, grid: np.ndarray) -> None:

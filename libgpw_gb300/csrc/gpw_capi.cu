@@ -945,9 +945,47 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
         }
     }
     gd.ortho = use_ortho ? 1 : 0;
-    gpw_plan *P = nullptr;
-    int st = gpw_plan_create(&P, 1, &gd, dev);
-    if (st) return st;
+    // The reference's callers make this call once per pair, many times over the
+    // same grid: the plan (one per grid geometry) and the device buffers stay in a
+    // per-thread cache, so a call is the host set-up, three copies, two launches.
+    struct Cache {
+        int device = -1;
+        gpw_grid_desc desc;
+        gpw_plan *plan = nullptr;
+        PairGeom *d_geom = nullptr;
+        int *d_status = nullptr;
+        int *d_table = nullptr;
+        double *d_coef = nullptr, *d_pab = nullptr, *d_grid = nullptr;
+        size_t cap_table = 0, cap_pab = 0, cap_grid = 0;
+        std::vector<int> table;
+        ~Cache() { release(); }
+        void release() {
+            if (plan) gpw_plan_destroy(plan);
+            cudaFree(d_geom);
+            cudaFree(d_status);
+            cudaFree(d_table);
+            cudaFree(d_coef);
+            cudaFree(d_pab);
+            cudaFree(d_grid);
+            plan = nullptr;
+            d_geom = nullptr;
+            d_status = nullptr;
+            d_table = nullptr;
+            d_coef = d_pab = d_grid = nullptr;
+            cap_table = cap_pab = cap_grid = 0;
+        }
+    };
+    thread_local Cache C;
+    if (!C.plan || C.device != dev || memcmp(&C.desc, &gd, sizeof gd) != 0) {
+        C.release();
+        int st = gpw_plan_create(&C.plan, 1, &gd, dev);
+        if (st) return st;
+        C.device = dev;
+        C.desc = gd;
+        GPW_CUDA(cudaMalloc(&C.d_geom, sizeof(PairGeom)));
+        GPW_CUDA(cudaMalloc(&C.d_status, sizeof(int)));
+        GPW_CUDA(cudaMalloc(&C.d_coef, sizeof(double) * ncoef(kMaxLp)));
+    }
     gpw_task t;
     memset(&t, 0, sizeof t);
     t.zeta = zeta; t.zetb = zetb; t.rscale = rscale;
@@ -959,19 +997,49 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
     t.sphere_offset = use_ortho ? 0 : -1;
     if (use_ortho)
         for (int i = 0; i < 3; i++) { t.lb_cube[i] = lb_cube[i]; t.ub_cube[i] = ub_cube[i]; }
-    gpw_taskset *T = nullptr;
-    st = gpw_taskset_create(P, &t, 1, compute_tau ? GPW_FUNC_DADB : GPW_FUNC_AB, use_ortho ? sphere_bounds : nullptr,
-                            use_ortho ? nspheres : 0, &T);
-    if (st == GPW_SUCCESS) {
-        // the block is read at (o2+jco)*maxco + o1+ico < maxco*maxco
-        double *gp[1] = {grid};
-        std::vector<double> blk(pab, pab + (size_t)maxco * maxco);
-        if (T->pab_extent > (int64_t)blk.size()) blk.resize((size_t)T->pab_extent, 0.0);
-        st = gpw_collocate_host(T, GPW_PREC_FP64, blk.data(), gp);
-    }
-    gpw_taskset_destroy(T);
-    gpw_plan_destroy(P);
-    return st;
+    const int func = compute_tau ? GPW_FUNC_DADB : GPW_FUNC_AB;
+    PairGeom g;
+    C.table.clear();
+    int st = make_geom(t, 0, *C.plan, func, use_ortho ? sphere_bounds : nullptr, use_ortho ? nspheres : 0, g,
+                       C.table);
+    if (st) return st;
+    g.coef_off = 0;
+    g.mom_ext_off = 0;
+    // the block is read at (o2+jco)*maxco + o1+ico < maxco*maxco
+    const size_t npab = (size_t)maxco * maxco;
+    const size_t ngr = (size_t)C.plan->lv[0].grid_elems;
+    int smem_limit = 0;
+    cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if ((g.ortho ? smem_ortho_fp64(g) : smem_general_fp64(g)) > smem_limit || smem_prep(g.la_max, g.lb_max) > smem_limit)
+        return fail(GPW_ERR_UNSUPPORTED, "gpw_collocate_pgf_product_rspace: a cube is too large for one CTA");
+    auto grow = [&](auto **p, size_t &cap, size_t need) -> cudaError_t {
+        if (need <= cap) return cudaSuccess;
+        cudaFree(*p);
+        *p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc((void **)p, sizeof(**p) * need);
+        if (e == cudaSuccess) cap = need;
+        return e;
+    };
+    GPW_CUDA(grow(&C.d_table, C.cap_table, std::max<size_t>(C.table.size(), 1)));
+    GPW_CUDA(grow(&C.d_pab, C.cap_pab, npab));
+    GPW_CUDA(grow(&C.d_grid, C.cap_grid, ngr));
+    cudaStream_t s = nullptr;
+    GPW_CUDA(cudaMemcpyAsync(C.d_geom, &g, sizeof g, cudaMemcpyHostToDevice, s));
+    if (!C.table.empty())
+        GPW_CUDA(cudaMemcpyAsync(C.d_table, C.table.data(), sizeof(int) * C.table.size(), cudaMemcpyHostToDevice, s));
+    GPW_CUDA(cudaMemcpyAsync(C.d_pab, pab, sizeof(double) * npab, cudaMemcpyHostToDevice, s));
+    GPW_CUDA(cudaMemcpyAsync(C.d_grid, grid, sizeof(double) * ngr, cudaMemcpyHostToDevice, s));
+    GPW_CUDA(cudaMemsetAsync(C.d_status, 0, sizeof(int), s));
+    GPW_CUDA(launch_one_fp64(g, C.d_geom, C.plan->d_levels, C.plan->d_tmat, C.d_table, C.d_coef, C.d_status, func,
+                             C.d_pab, C.d_grid, s));
+    int h = 0;
+    GPW_CUDA(cudaMemcpyAsync(grid, C.d_grid, sizeof(double) * ngr, cudaMemcpyDeviceToHost, s));
+    GPW_CUDA(cudaMemcpyAsync(&h, C.d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPW_CUDA(cudaStreamSynchronize(s));
+    if (h & kStatOutOfWindow) return fail(GPW_ERR_OUT_OF_WINDOW, "a cube left the local grid window");
+    if (h) return fail(GPW_ERR_INVALID_ARG, "gpw_collocate_pgf_product_rspace: device status " + std::to_string(h));
+    return GPW_SUCCESS;
 }
 
 int gpw_selftest_tensorcore(int64_t *mismatches) {
@@ -980,6 +1048,16 @@ int gpw_selftest_tensorcore(int64_t *mismatches) {
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GPW_ERR_NO_DEVICE, "no CUDA device");
     std::string err;
     const int st = tc_selftest(mismatches, err);
+    return st ? fail(st, err) : GPW_SUCCESS;
+}
+
+int gpw_selftest_ff_exp(int64_t npoints, double *max_rel_err, double *max_rel_err_low) {
+    if (!max_rel_err || !max_rel_err_low || npoints < 16) return fail(GPW_ERR_INVALID_ARG, "gpw_selftest_ff_exp: bad arguments");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GPW_ERR_NO_DEVICE, "no CUDA device");
+    std::string err;
+    double arg = 0.0;
+    const int st = ffexp_selftest(npoints, max_rel_err, max_rel_err_low, &arg, err);
     return st ? fail(st, err) : GPW_SUCCESS;
 }
 

@@ -721,6 +721,25 @@ cudaError_t launch_pairs_fp64(const PairGeom *d_geoms, const LevelDev *d_levels,
     return cudaGetLastError();
 }
 
+// One pair from raw device pointers, orthorhombic (with its cube list in d_table
+// when the pair has one) or general cell: set-up, then the FP64 collocation.
+cudaError_t launch_one_fp64(const PairGeom &g, const PairGeom *d_geom, const LevelDev *d_levels, const double *d_tmat,
+                            const int *d_table, double *d_coef, int *d_status, int func, const double *d_pab,
+                            double *d_grid, cudaStream_t s) {
+    k_prep<<<1, 128, smem_prep(g.la_max, g.lb_max), s>>>(d_geom, d_levels, d_tmat, func, d_pab, d_coef);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    GridPtrs gp;
+    for (int l = 0; l < GPW_MAX_LEVELS; l++) gp.p[l] = d_grid;
+    if (g.ortho)
+        k_ortho_fp64<false><<<1, 256, smem_ortho_fp64(g), s>>>(d_geom, 0, d_levels, d_table, d_coef, nullptr, gp,
+                                                             d_status, 0);
+    else
+        k_general_fp64<false><<<1, 256, smem_general_fp64(g), s>>>(d_geom, 0, d_levels, d_coef, nullptr, gp,
+                                                                  d_status, 0);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_collocate_fp64(const TaskSet &ts, const GridPtrs &g, cudaStream_t s) {
     return launch_fp64_kind(ts, g, false, -1, s);
 }

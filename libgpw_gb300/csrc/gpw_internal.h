@@ -127,8 +127,14 @@ cudaError_t launch_pairs_fp64(const PairGeom *d_geoms, const LevelDev *d_levels,
                               double *d_coef, int *d_status, int n, int tau, int max_A, int max_B,
                               int smem_coll, const double *d_pab, double *d_grid, cudaStream_t s);
 
+// gpw_fp64.cu: one pair (the drop-in entry): set-up + collocation from raw device pointers
+cudaError_t launch_one_fp64(const PairGeom &g, const PairGeom *d_geom, const LevelDev *d_levels, const double *d_tmat,
+                            const int *d_table, double *d_coef, int *d_status, int func, const double *d_pab,
+                            double *d_grid, cudaStream_t s);
+
 // gpw_selftest.cu
 int tc_selftest(int64_t *mismatches, std::string &err);
+int ffexp_selftest(int64_t n, double *err_normal, double *err_low, double *arg_normal, std::string &err);
 
 // gpw_backward.cu
 cudaError_t launch_backward(const TaskSet &ts, const double *d_pab, const GridPtrs &g,

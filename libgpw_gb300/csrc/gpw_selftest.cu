@@ -6,9 +6,11 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <random>
 #include <vector>
 
+#include "gpw_ff.cuh"
 #include "gpw_internal.h"
 #include "gpw_tc.cuh"
 
@@ -121,6 +123,60 @@ int tc_selftest(int64_t *mismatches, std::string &err) {
             if ((double)D[m * 32 + n] != s) bad++;
         }
     *mismatches = bad;
+    return GPW_SUCCESS;
+}
+
+// ff_exp sweep: n arguments spread over [lo, hi) in float-float (a low part of up
+// to half an ulp of the high part), each compared with the FP64 exp of the same
+// value; the largest relative error and its argument per range.
+__global__ void k_ffexp_sweep(int64_t n, double lo, double hi, unsigned long long *max_bits, double *arg) {
+    double worst = 0.0, where = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double x = lo + (hi - lo) * ((double)i / (double)n);
+        const float xh = __double2float_rn(x);
+        // low part: a pseudo-random fraction of half an ulp of the high part
+        const uint32_t h = (uint32_t)(i * 2654435761ull) >> 8;
+        const float ulp = fabsf(__int_as_float(__float_as_int(xh) + 1) - xh);
+        const float xl = ((float)h / 16777216.0f - 0.5f) * ulp;
+        const ff v = ff_exp(ff{xh, xl});
+        const double ref = exp((double)xh + (double)xl);
+        const double err = fabs(((double)v.hi + (double)v.lo) - ref) / ref;
+        if (err > worst) {
+            worst = err;
+            where = (double)xh + (double)xl;
+        }
+    }
+    // non-negative doubles order as their bit patterns
+    const unsigned long long wb = (unsigned long long)__double_as_longlong(worst);
+    if (atomicMax(max_bits, wb) < wb) *arg = where;  // the argument is approximate under races
+}
+
+int ffexp_selftest(int64_t n, double *err_normal, double *err_low, double *arg_normal, std::string &err) {
+    unsigned long long *d_bits = nullptr;
+    double *d_arg = nullptr;
+    cudaError_t e = cudaMalloc(&d_bits, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&d_arg, 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(d_bits, 0, 2 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(d_arg, 0, 2 * sizeof(double));
+    if (e == cudaSuccess) {
+        // results with a normal low part (a > -60), then the range where it underflows gradually
+        k_ffexp_sweep<<<1024, 256>>>(n, -60.0, 88.0, d_bits, d_arg);
+        k_ffexp_sweep<<<1024, 256>>>(n / 4, -103.0, -60.0, d_bits + 1, d_arg + 1);
+        e = cudaGetLastError();
+    }
+    unsigned long long bits[2] = {0, 0};
+    double args[2] = {0, 0};
+    if (e == cudaSuccess) e = cudaMemcpy(bits, d_bits, sizeof bits, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(args, d_arg, sizeof args, cudaMemcpyDeviceToHost);
+    cudaFree(d_bits);
+    cudaFree(d_arg);
+    if (e != cudaSuccess) {
+        err = std::string("ffexp_selftest: ") + cudaGetErrorString(e);
+        return GPW_ERR_CUDA;
+    }
+    memcpy(err_normal, &bits[0], sizeof(double));
+    memcpy(err_low, &bits[1], sizeof(double));
+    *arg_normal = args[0];
     return GPW_SUCCESS;
 }
 
