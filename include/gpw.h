@@ -253,7 +253,8 @@ int gpw_selftest_tensorcore(int64_t *mismatches);
  * each a float-float value (a low part of up to half an ulp), against the FP64
  * exp of the same value on the current device.  *max_rel_err receives the
  * largest relative error where the result has a normal low part (a > -60),
- * *max_rel_err_low the largest below (the low part underflows gradually there).
+ * *max_rel_err_low the largest error below, relative to max(exp(a), 2^-126):
+ * there the low part, and below a = -87.3 the high part too, are subnormal.
  */
 int gpw_selftest_ff_exp(int64_t npoints, double *max_rel_err, double *max_rel_err_low);
 

@@ -948,31 +948,29 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
     // The reference's callers make this call once per pair, many times over the
     // same grid: the plan (one per grid geometry) and the device buffers stay in a
     // per-thread cache, so a call is the host set-up, three copies, two launches.
+    // The reference's callers make this call once per pair, many times over the
+    // same grid: the plan (one per grid geometry), a device buffer and a pinned
+    // host mirror of it stay in a per-thread cache, so a call is the host set-up,
+    // one copy in (geometry, cube list, block, grid), two launches and one copy
+    // out (status word and grid).
     struct Cache {
         int device = -1;
         gpw_grid_desc desc;
         gpw_plan *plan = nullptr;
-        PairGeom *d_geom = nullptr;
-        int *d_status = nullptr;
-        int *d_table = nullptr;
-        double *d_coef = nullptr, *d_pab = nullptr, *d_grid = nullptr;
-        size_t cap_table = 0, cap_pab = 0, cap_grid = 0;
+        double *d_coef = nullptr;
+        unsigned char *d_buf = nullptr, *h_buf = nullptr;
+        size_t cap = 0;
         std::vector<int> table;
         ~Cache() { release(); }
         void release() {
             if (plan) gpw_plan_destroy(plan);
-            cudaFree(d_geom);
-            cudaFree(d_status);
-            cudaFree(d_table);
             cudaFree(d_coef);
-            cudaFree(d_pab);
-            cudaFree(d_grid);
+            cudaFree(d_buf);
+            if (h_buf) cudaFreeHost(h_buf);
             plan = nullptr;
-            d_geom = nullptr;
-            d_status = nullptr;
-            d_table = nullptr;
-            d_coef = d_pab = d_grid = nullptr;
-            cap_table = cap_pab = cap_grid = 0;
+            d_coef = nullptr;
+            d_buf = h_buf = nullptr;
+            cap = 0;
         }
     };
     thread_local Cache C;
@@ -982,8 +980,6 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
         if (st) return st;
         C.device = dev;
         C.desc = gd;
-        GPW_CUDA(cudaMalloc(&C.d_geom, sizeof(PairGeom)));
-        GPW_CUDA(cudaMalloc(&C.d_status, sizeof(int)));
         GPW_CUDA(cudaMalloc(&C.d_coef, sizeof(double) * ncoef(kMaxLp)));
     }
     gpw_task t;
@@ -1012,31 +1008,39 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
     cudaDeviceGetAttribute(&smem_limit, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     if ((g.ortho ? smem_ortho_fp64(g) : smem_general_fp64(g)) > smem_limit || smem_prep(g.la_max, g.lb_max) > smem_limit)
         return fail(GPW_ERR_UNSUPPORTED, "gpw_collocate_pgf_product_rspace: a cube is too large for one CTA");
-    auto grow = [&](auto **p, size_t &cap, size_t need) -> cudaError_t {
-        if (need <= cap) return cudaSuccess;
-        cudaFree(*p);
-        *p = nullptr;
-        cap = 0;
-        cudaError_t e = cudaMalloc((void **)p, sizeof(**p) * need);
-        if (e == cudaSuccess) cap = need;
-        return e;
-    };
-    GPW_CUDA(grow(&C.d_table, C.cap_table, std::max<size_t>(C.table.size(), 1)));
-    GPW_CUDA(grow(&C.d_pab, C.cap_pab, npab));
-    GPW_CUDA(grow(&C.d_grid, C.cap_grid, ngr));
+    // buffer layout: geometry | cube list | block | status word | grid (256-byte aligned parts)
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t o_table = al(sizeof(PairGeom));
+    const size_t o_pab = al(o_table + sizeof(int) * std::max<size_t>(C.table.size(), 1));
+    const size_t o_stat = al(o_pab + sizeof(double) * npab);
+    const size_t o_grid = o_stat + 256;
+    const size_t total = o_grid + sizeof(double) * ngr;
+    if (total > C.cap) {
+        cudaFree(C.d_buf);
+        if (C.h_buf) cudaFreeHost(C.h_buf);
+        C.d_buf = C.h_buf = nullptr;
+        C.cap = 0;
+        GPW_CUDA(cudaMalloc(&C.d_buf, total));
+        GPW_CUDA(cudaHostAlloc(&C.h_buf, total, cudaHostAllocDefault));
+        C.cap = total;
+    }
+    memcpy(C.h_buf, &g, sizeof g);
+    if (!C.table.empty()) memcpy(C.h_buf + o_table, C.table.data(), sizeof(int) * C.table.size());
+    memcpy(C.h_buf + o_pab, pab, sizeof(double) * npab);
+    memset(C.h_buf + o_stat, 0, sizeof(int));
+    memcpy(C.h_buf + o_grid, grid, sizeof(double) * ngr);
     cudaStream_t s = nullptr;
-    GPW_CUDA(cudaMemcpyAsync(C.d_geom, &g, sizeof g, cudaMemcpyHostToDevice, s));
-    if (!C.table.empty())
-        GPW_CUDA(cudaMemcpyAsync(C.d_table, C.table.data(), sizeof(int) * C.table.size(), cudaMemcpyHostToDevice, s));
-    GPW_CUDA(cudaMemcpyAsync(C.d_pab, pab, sizeof(double) * npab, cudaMemcpyHostToDevice, s));
-    GPW_CUDA(cudaMemcpyAsync(C.d_grid, grid, sizeof(double) * ngr, cudaMemcpyHostToDevice, s));
-    GPW_CUDA(cudaMemsetAsync(C.d_status, 0, sizeof(int), s));
-    GPW_CUDA(launch_one_fp64(g, C.d_geom, C.plan->d_levels, C.plan->d_tmat, C.d_table, C.d_coef, C.d_status, func,
-                             C.d_pab, C.d_grid, s));
-    int h = 0;
-    GPW_CUDA(cudaMemcpyAsync(grid, C.d_grid, sizeof(double) * ngr, cudaMemcpyDeviceToHost, s));
-    GPW_CUDA(cudaMemcpyAsync(&h, C.d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GPW_CUDA(cudaMemcpyAsync(C.d_buf, C.h_buf, total, cudaMemcpyHostToDevice, s));
+    int *d_status = reinterpret_cast<int *>(C.d_buf + o_stat);
+    double *d_grid = reinterpret_cast<double *>(C.d_buf + o_grid);
+    GPW_CUDA(launch_one_fp64(g, reinterpret_cast<PairGeom *>(C.d_buf), C.plan->d_levels, C.plan->d_tmat,
+                             reinterpret_cast<int *>(C.d_buf + o_table), C.d_coef, d_status, func,
+                             reinterpret_cast<double *>(C.d_buf + o_pab), d_grid, s));
+    GPW_CUDA(cudaMemcpyAsync(C.h_buf + o_stat, C.d_buf + o_stat, total - o_stat, cudaMemcpyDeviceToHost, s));
     GPW_CUDA(cudaStreamSynchronize(s));
+    int h = 0;
+    memcpy(&h, C.h_buf + o_stat, sizeof(int));
+    memcpy(grid, C.h_buf + o_grid, sizeof(double) * ngr);
     if (h & kStatOutOfWindow) return fail(GPW_ERR_OUT_OF_WINDOW, "a cube left the local grid window");
     if (h) return fail(GPW_ERR_INVALID_ARG, "gpw_collocate_pgf_product_rspace: device status " + std::to_string(h));
     return GPW_SUCCESS;
@@ -1056,8 +1060,7 @@ int gpw_selftest_ff_exp(int64_t npoints, double *max_rel_err, double *max_rel_er
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(GPW_ERR_NO_DEVICE, "no CUDA device");
     std::string err;
-    double arg = 0.0;
-    const int st = ffexp_selftest(npoints, max_rel_err, max_rel_err_low, &arg, err);
+    const int st = ffexp_selftest(npoints, max_rel_err, max_rel_err_low, err);
     return st ? fail(st, err) : GPW_SUCCESS;
 }
 

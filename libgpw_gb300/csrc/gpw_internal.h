@@ -134,7 +134,7 @@ cudaError_t launch_one_fp64(const PairGeom &g, const PairGeom *d_geom, const Lev
 
 // gpw_selftest.cu
 int tc_selftest(int64_t *mismatches, std::string &err);
-int ffexp_selftest(int64_t n, double *err_normal, double *err_low, double *arg_normal, std::string &err);
+int ffexp_selftest(int64_t n, double *err_normal, double *err_low, std::string &err);
 
 // gpw_backward.cu
 cudaError_t launch_backward(const TaskSet &ts, const double *d_pab, const GridPtrs &g,

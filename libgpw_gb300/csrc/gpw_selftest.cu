@@ -6,6 +6,7 @@
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <random>
 #include <vector>
@@ -128,9 +129,9 @@ int tc_selftest(int64_t *mismatches, std::string &err) {
 
 // ff_exp sweep: n arguments spread over [lo, hi) in float-float (a low part of up
 // to half an ulp of the high part), each compared with the FP64 exp of the same
-// value; the largest relative error and its argument per range.
-__global__ void k_ffexp_sweep(int64_t n, double lo, double hi, unsigned long long *max_bits, double *arg) {
-    double worst = 0.0, where = 0.0;
+// value; every thread writes the largest error it saw (host reduction).
+__global__ void k_ffexp_sweep(int64_t n, double lo, double hi, double *worst_out) {
+    double worst = 0.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double x = lo + (hi - lo) * ((double)i / (double)n);
         const float xh = __double2float_rn(x);
@@ -140,43 +141,37 @@ __global__ void k_ffexp_sweep(int64_t n, double lo, double hi, unsigned long lon
         const float xl = ((float)h / 16777216.0f - 0.5f) * ulp;
         const ff v = ff_exp(ff{xh, xl});
         const double ref = exp((double)xh + (double)xl);
-        const double err = fabs(((double)v.hi + (double)v.lo) - ref) / ref;
-        if (err > worst) {
-            worst = err;
-            where = (double)xh + (double)xl;
-        }
+        // relative to exp, or to the smallest normal float where exp is below it
+        // (results there are float subnormals with only a few significant bits)
+        worst = fmax(worst, fabs(((double)v.hi + (double)v.lo) - ref) / fmax(ref, 0x1p-126));
     }
-    // non-negative doubles order as their bit patterns
-    const unsigned long long wb = (unsigned long long)__double_as_longlong(worst);
-    if (atomicMax(max_bits, wb) < wb) *arg = where;  // the argument is approximate under races
+    worst_out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = worst;
 }
 
-int ffexp_selftest(int64_t n, double *err_normal, double *err_low, double *arg_normal, std::string &err) {
-    unsigned long long *d_bits = nullptr;
-    double *d_arg = nullptr;
-    cudaError_t e = cudaMalloc(&d_bits, 2 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc(&d_arg, 2 * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemset(d_bits, 0, 2 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMemset(d_arg, 0, 2 * sizeof(double));
+int ffexp_selftest(int64_t n, double *err_normal, double *err_low, std::string &err) {
+    constexpr int kBlocks = 1024, kThreads = 256, kN = kBlocks * kThreads;
+    double *d_w = nullptr;
+    cudaError_t e = cudaMalloc(&d_w, 2 * sizeof(double) * kN);
     if (e == cudaSuccess) {
         // results with a normal low part (a > -60), then the range where it underflows gradually
-        k_ffexp_sweep<<<1024, 256>>>(n, -60.0, 88.0, d_bits, d_arg);
-        k_ffexp_sweep<<<1024, 256>>>(n / 4, -103.0, -60.0, d_bits + 1, d_arg + 1);
+        k_ffexp_sweep<<<kBlocks, kThreads>>>(n, -60.0, 88.0, d_w);
+        k_ffexp_sweep<<<kBlocks, kThreads>>>(n / 4, -103.0, -60.0, d_w + kN);
         e = cudaGetLastError();
     }
-    unsigned long long bits[2] = {0, 0};
-    double args[2] = {0, 0};
-    if (e == cudaSuccess) e = cudaMemcpy(bits, d_bits, sizeof bits, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(args, d_arg, sizeof args, cudaMemcpyDeviceToHost);
-    cudaFree(d_bits);
-    cudaFree(d_arg);
+    std::vector<double> w(2 * (size_t)kN, 0.0);
+    if (e == cudaSuccess) e = cudaMemcpy(w.data(), d_w, sizeof(double) * w.size(), cudaMemcpyDeviceToHost);
+    cudaFree(d_w);
     if (e != cudaSuccess) {
         err = std::string("ffexp_selftest: ") + cudaGetErrorString(e);
         return GPW_ERR_CUDA;
     }
-    memcpy(err_normal, &bits[0], sizeof(double));
-    memcpy(err_low, &bits[1], sizeof(double));
-    *arg_normal = args[0];
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < kN; i++) {
+        a = std::max(a, w[i]);
+        b = std::max(b, w[kN + i]);
+    }
+    *err_normal = a;
+    *err_low = b;
     return GPW_SUCCESS;
 }
 
