@@ -140,14 +140,12 @@ class Clocks:
 
 
 # ----------------------------------------------------------------------------
-# DRAM bytes (read + write) of one launch of each tiled kernel on the 1M-pair
-# workload: dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture of
-# the build these constants were last measured with (the committed profile summary
-# gives the command and the date); None where not captured for the current build.
-TRAFFIC = {
-    ("pairs1M_l4_256cubed", 1000000, "k_collocate_tiled"): 19.678038e9 + 0.326584e9,
-    ("pairs1M_l4_256cubed", 1000000, "k_integrate_tiled"): 20.574986e9 + 8.899182e9,
-}
+# DRAM bytes (read + write) per (tile, pair) item of each tiled kernel:
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 3,000-pair
+# sample of the 1M-pair workload (256^3), divided by that launch's items; a launch's
+# traffic is estimated as this times its items (the committed profile summaries give
+# the captures and their item counts).
+TRAFFIC_PER_ITEM = {"k_collocate_tiled": None, "k_integrate_tiled": None}
 
 
 def algorithmic_flops(wl) -> tuple:
@@ -312,6 +310,7 @@ def main():
     plan = capi.Plan(wl.levels, device=local)
     ts = capi.TaskSet.from_workload(plan, wl)
     plan_s = time.perf_counter() - t0
+    items, units = ts.bins()
     # a geometry step of the same pairs: centres moved (device set-up and re-binning,
     # gpw_taskset_update_geometry), then moved back to the benchmark's geometry; the
     # second update is the one reported (the first also allocates its buffers)
@@ -480,7 +479,10 @@ def main():
         peak = peaks.get("bf16_tflops_sustained") or 1700.0
         kname = f"k_{dom}_tiled"
         roof = {"bound": "tensor", "kernel": kname, "achieved": achieved_tf, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved_tf / peak, "traffic": TRAFFIC.get((wl.name, wl.ntasks, kname)),
+                "frac": achieved_tf / peak,
+                "traffic": TRAFFIC_PER_ITEM[kname] * items if TRAFFIC_PER_ITEM.get(kname) else None,
+                "traffic_basis": "bytes per item of the 3,000-pair capture x this launch's items",
+                "items_per_launch": items,
                 "peak_source": "bf16 sustained, MEASURED_PEAKS.json (of measured)",
                 "limiter": "FP32/integer instruction issue of the float-float stages, not the tensor pipe "
                            "(tensor pipe active ~4%, issue slots busy 61% collocate / 52% integrate in the ncu captures)"}
@@ -523,7 +525,7 @@ def main():
                    "l2": "grid and potential exceed L2; a 512 MB buffer is written between timed steps",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                    "launch": "CUDA graph replay of the step" if graph is not None else "direct launches",
-                   "plan_seconds": plan_s, "geometry_update_ms": geo_ms[-1] if geo_ms else None, "tile_z": tiles, "tile_source": tile_src, "tune_seconds": tune_s},
+                   "plan_seconds": plan_s, "items": items, "units": units, "geometry_update_ms": geo_ms[-1] if geo_ms else None, "tile_z": tiles, "tile_source": tile_src, "tune_seconds": tune_s},
         "gpu_launches": int(n_kernels * args.steps),
         "roofline": roof, "error": err, "vs_fp64": vs_fp64, "clocks": clk.summary(), "cpu_baseline": cpu,
         "e2e": e2e,

@@ -210,6 +210,9 @@ int gpw_taskset_update_geometry(gpw_taskset *ts, const double *d_ra, const doubl
  * three.  Any output pointer may be NULL.
  */
 int gpw_taskset_profile(gpw_taskset *ts, int enable);
+/* Diagnostics of the tiled path: its (tile, pair) items and work units (0 and
+ * 0 when the task set has no tiled pairs). */
+int gpw_taskset_bins(const gpw_taskset *ts, int64_t *items, int64_t *units);
 int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms,
                       int64_t *contraction_launches, int64_t *kernel_launches);
 

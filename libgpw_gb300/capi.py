@@ -65,6 +65,7 @@ def lib():
         "gpw_collocate_pgf_product_rspace": ([i32] * 6 + [dbl] * 3 + [vp] * 8 + [i32, dbl, vp, vp, i32, vp, i32,
                                                                                 i32, i32, vp, vp], i32),
         "gpw_taskset_profile": ([vp, i32], i32),
+        "gpw_taskset_bins": ([vp, C.POINTER(i64), C.POINTER(i64)], i32),
         "gpw_taskset_stats": ([vp, C.POINTER(dbl), C.POINTER(i64), C.POINTER(i64)], i32),
         "gpw_taskset_set_tiles": ([vp, vp], i32),
         "gpw_taskset_get_tiles": ([vp, vp], i32),
@@ -216,6 +217,12 @@ class TaskSet:
         ms, nc, nk = C.c_double(), C.c_int64(), C.c_int64()
         check(lib().gpw_taskset_stats(self.handle, C.byref(ms), C.byref(nc), C.byref(nk)), "gpw_taskset_stats")
         return ms.value, nc.value, nk.value
+
+    def bins(self) -> tuple:
+        """(tile, pair) items and work units of the tiled path (gpw_taskset_bins)."""
+        a, b = C.c_int64(), C.c_int64()
+        check(lib().gpw_taskset_bins(self.handle, C.byref(a), C.byref(b)), "gpw_taskset_bins")
+        return a.value, b.value
 
     def check(self, stream=None):
         check(lib().gpw_taskset_check(self.handle, _stream_handle(stream)), "device status")

@@ -849,6 +849,13 @@ int gpw_taskset_profile(gpw_taskset *ts, int enable) {
     return GPW_SUCCESS;
 }
 
+int gpw_taskset_bins(const gpw_taskset *ts, int64_t *items, int64_t *units) {
+    if (!ts) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_bins: null");
+    if (items) *items = mixed_items(*ts);
+    if (units) *units = mixed_units(*ts);
+    return GPW_SUCCESS;
+}
+
 int gpw_taskset_stats(gpw_taskset *ts, double *contraction_ms, int64_t *contraction_launches,
                       int64_t *kernel_launches) {
     if (!ts) return fail(GPW_ERR_INVALID_ARG, "gpw_taskset_stats: null");

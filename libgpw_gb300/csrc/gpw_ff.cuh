@@ -8,7 +8,9 @@
 
 namespace gpw {
 
-struct ff {
+// 8-byte aligned, so that shared-memory arrays of ff load and store as one
+// 64-bit access per element
+struct alignas(8) ff {
     float hi, lo;
 };
 

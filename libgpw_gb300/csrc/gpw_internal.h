@@ -111,6 +111,8 @@ cudaError_t launch_integrate_core(const int length[3], int L, const double *pol,
 // gpw_mixed.cu
 int mixed_build(TaskSet &ts, std::string &err);
 int mixed_rebin(TaskSet &ts, std::string &err);  // records and bins from ts.d_geom
+int64_t mixed_items(const TaskSet &ts);           // (tile, pair) items of the tiled path
+int64_t mixed_units(const TaskSet &ts);           // its work units
 void mixed_free(TaskSet &ts);
 cudaError_t launch_collocate_mixed(const TaskSet &ts, const GridPtrs &g, cudaStream_t s);
 cudaError_t launch_general_ff(const TaskSet &ts, const GridPtrs &g, bool adj, cudaStream_t s);

@@ -42,6 +42,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <numeric>
 #include <string>
@@ -111,9 +112,9 @@ constexpr int kCoef16Max = (NCOEF_MAX * (int)sizeof(float2) + 15) / 16;
 
 // the current periodic image of a pair over the tile
 struct ImgState {
+    ff tc;              // collocate: x of the re-expansion column minus xp
     int o[3];           // cube offset of the tile origin
     int gx0, gx1;       // tile-local x range inside the cube box
-    ff tc;              // collocate: x of the re-expansion column minus xp
     int ic;             // collocate: tile-local re-expansion column
     int sb;             // collocate: x-variable scale 2^sb of the slices (balancing)
 };
@@ -125,7 +126,6 @@ struct ImgState {
 struct alignas(16) ItemImg {
     ImgState im;
     int nimg;
-    int pad_[2];
 };
 static_assert(sizeof(ItemImg) == 48, "ItemImg is three 16-byte chunks");
 
@@ -1459,10 +1459,63 @@ __global__ void k_item_images(const TileDesc *__restrict__ tiles, const int64_t 
 // ---------------------------------------------------------------------------
 // Binning on the device: the (tile, pair) items of every binned pair.
 struct BinLevel {
+    double G[3][3];     // metric of the lattice steps, G_ab = v_a . v_b (general cells)
     int first;          // index of the level's first tile
     int nt[3];          // tiles per axis
     int lz;             // log2 of the tile z extent
 };
+
+// Minimum of d^T G d over the box lo <= d <= hi (G symmetric positive definite;
+// infinite bounds allowed).  The minimiser has every coordinate either free or
+// at one of its bounds; for each such pattern the stationary point of the free
+// coordinates is solved and, if it lies in the box, its value kept.  Rounding
+// can only accept a point just outside the box, which lowers the result: a test
+// "minimum > r^2" built on it never drops a point inside the sphere.
+__device__ double box_min_q(const double (&G)[3][3], const double (&lo)[3], const double (&hi)[3]) {
+    if (lo[0] <= 0.0 && hi[0] >= 0.0 && lo[1] <= 0.0 && hi[1] >= 0.0 && lo[2] <= 0.0 && hi[2] >= 0.0) return 0.0;
+    double best = HUGE_VAL;
+    for (int pat = 1; pat < 27; pat++) {  // pattern 0 (all free) is the origin, handled above
+        const int s[3] = {pat % 3, (pat / 3) % 3, pat / 9};  // 0 free, 1 at lo, 2 at hi
+        double d[3] = {0.0, 0.0, 0.0};
+        int fr[2], nf = 0;
+        bool ok = true;
+        for (int a = 0; a < 3; a++) {
+            if (s[a] == 0) {
+                fr[nf++] = a;
+            } else {
+                d[a] = s[a] == 1 ? lo[a] : hi[a];
+                ok = ok && isfinite(d[a]);
+            }
+        }
+        if (!ok) continue;
+        auto rhs = [&](int a) {  // -(G_aX d_X) over the fixed coordinates
+            double r = 0.0;
+            for (int b = 0; b < 3; b++)
+                if (s[b] != 0) r -= G[a][b] * d[b];
+            return r;
+        };
+        if (nf == 1) {
+            d[fr[0]] = rhs(fr[0]) / G[fr[0]][fr[0]];
+        } else if (nf == 2) {
+            const int a = fr[0], b = fr[1];
+            const double ra = rhs(a), rb = rhs(b);
+            const double det = G[a][a] * G[b][b] - G[a][b] * G[a][b];
+            d[a] = (ra * G[b][b] - rb * G[a][b]) / det;
+            d[b] = (G[a][a] * rb - G[a][b] * ra) / det;
+        }
+        for (int k = 0; k < nf; k++) {
+            const int a = fr[k];
+            const double tol = 1e-9 * (1.0 + fabs(d[a]));
+            ok = ok && d[a] >= lo[a] - tol && d[a] <= hi[a] + tol;
+        }
+        if (!ok) continue;
+        double q = 0.0;
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++) q += d[a] * G[a][b] * d[b];
+        best = fmin(best, q);
+    }
+    return best;
+}
 
 // One axis of a pair's cube (cube offsets lb..hi around cc, as grid_base_ref_c.cc:318-351
 // maps them) cut into runs of consecutive grid indices inside one tile.
@@ -1474,9 +1527,9 @@ struct AxisRuns {
         N = lv.ngrid[d]; npts = lv.npts[d]; periodic = lv.periodic[d]; lbg = lv.lb_grid[d];
         dedupe = periodic && (hi - lb + 1) + T > N;
     }
-    // the run starting at offset gg: its tile and the smallest folded offset |f|
-    // (f = g <= 0 ? -g : g - 1) over it; gg moves past the run; false: outside the window
-    __device__ bool next(int &gg, int &t, int &f) const {
+    // the run starting at offset gg: its tile and its offsets g0..g1; gg moves
+    // past the run; false: outside the window
+    __device__ bool next(int &gg, int &t, int &g0, int &g1) const {
         const int w = periodic ? imod(cc + gg, npts) : gg + imod(cc + lb + lbg, npts) - lb;
         if (w < 0 || w >= N) {
             gg++;
@@ -1484,28 +1537,57 @@ struct AxisRuns {
         }
         t = w / T;
         const int len = min(T - (w - t * T), N - w);
-        const int g1 = min(gg + len - 1, hi);
-        f = (gg <= 1 && g1 >= 0) ? 0 : (g1 < 0 ? -g1 : gg - 1);
+        g0 = gg;
+        g1 = min(gg + len - 1, hi);
         gg += len;
         return true;
     }
-    // calls fn(tile, fmin) once per tile the axis touches
+    // calls fn(tile, g0, g1) once per tile the axis touches; where several runs
+    // reach one tile, only the first reports it, with the hull of their offsets
     template <class Fn>
-    __device__ void each(Fn &&fn) const {
+    __device__ void each_range(Fn &&fn) const {
         for (int gg = lb; gg <= hi;) {
-            const int g0 = gg;
-            int t, f;
-            if (!next(gg, t, f)) continue;
-            if (dedupe) {  // only the first run into a tile reports it, with the minimum over all runs
+            const int gs = gg;
+            int t, g0, g1;
+            if (!next(gg, t, g0, g1)) continue;
+            if (dedupe) {
                 bool seen = false;
-                for (int g2 = lb; g2 < g0 && !seen;) {
-                    int t2, f2;
-                    if (next(g2, t2, f2) && t2 == t) seen = true;
+                for (int g2 = lb; g2 < gs && !seen;) {
+                    int t2, a2, b2;
+                    if (next(g2, t2, a2, b2) && t2 == t) seen = true;
                 }
                 if (seen) continue;
                 for (int g2 = gg; g2 <= hi;) {
-                    int t2, f2;
-                    if (next(g2, t2, f2) && t2 == t) f = min(f, f2);
+                    int t2, a2, b2;
+                    if (next(g2, t2, a2, b2) && t2 == t) {
+                        g0 = min(g0, a2);
+                        g1 = max(g1, b2);
+                    }
+                }
+            }
+            fn(t, g0, g1);
+        }
+    }
+    // calls fn(tile, fmin) once per tile the axis touches, fmin the smallest folded
+    // offset |f| (f = g <= 0 ? -g : g - 1) over the runs into the tile
+    template <class Fn>
+    __device__ void each(Fn &&fn) const {
+        for (int gg = lb; gg <= hi;) {
+            const int gs = gg;
+            int t, g0, g1;
+            if (!next(gg, t, g0, g1)) continue;
+            auto fold = [](int a, int b) { return (a <= 1 && b >= 0) ? 0 : (b < 0 ? -b : a - 1); };
+            int f = fold(g0, g1);
+            if (dedupe) {  // only the first run into a tile reports it, with the minimum over all runs
+                bool seen = false;
+                for (int g2 = lb; g2 < gs && !seen;) {
+                    int t2, a2, b2;
+                    if (next(g2, t2, a2, b2) && t2 == t) seen = true;
+                }
+                if (seen) continue;
+                for (int g2 = gg; g2 <= hi;) {
+                    int t2, a2, b2;
+                    if (next(g2, t2, a2, b2) && t2 == t) f = min(f, fold(a2, b2));
                 }
             }
             fn(t, f);
@@ -1515,8 +1597,10 @@ struct AxisRuns {
 
 // Pass 0: items per tile (count).  Pass 1: item words into the tile's slots
 // (cursor).  A pair visits a tile only if some cube point of the tile can be
-// inside its sphere: folded distance of the tile's nearest offsets <= radius
-// (with a margin); explicit cube lists and general-cell boxes are not culled.
+// inside its sphere (with a margin): orthorhombic, the folded distance of the
+// tile's nearest offsets <= radius; general cell, the least |r - rp|^2 over the
+// lattice-index box of the tile's offsets (box_min_q) <= radius^2, tested per z
+// run, then per (z, y) runs, then per tile.  Explicit cube lists are not culled.
 __global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, const LevelDev *__restrict__ levels,
                             const BinLevel *__restrict__ bl, const int64_t *__restrict__ off16,
                             const int *__restrict__ len16, int pass, int *count, unsigned long long *cursor,
@@ -1537,8 +1621,40 @@ __global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, co
         az.init(lv, 2, g.cc[2], lb[2], hi[2], sh.TZ);
         const double r2 = g.radius * g.radius * (1.0 + 1e-9) + 1e-12;
         const double hx = lv.dh[0][0], hy = lv.dh[1][1], hz = lv.dh[2][2];
-        const bool table = g.table_off >= 0 || !g.ortho;
+        const bool table = g.table_off >= 0;
         const uint64_t word = ((uint64_t)off16[k] << 16) | (uint64_t)len16[k];
+        auto emit = [&](int tz, int ty, int tx) {
+            const int tile = B.first + (tz * B.nt[1] + ty) * B.nt[0] + tx;
+            if (pass == 0) atomicAdd(count + tile, 1);
+            else items[atomicAdd(cursor + tile, 1ull)] = word;
+        };
+        if (!g.ortho) {
+            // lattice-index offsets from the product centre: d_a = cc_a + gg - gp_a
+            const double c[3] = {g.off[0] - g.cc[0], g.off[1] - g.cc[1], g.off[2] - g.cc[2]};
+            const double rg = g.radius * g.radius * (1.0 + 1e-6) + 1e-12;
+            double lo[3] = {-HUGE_VAL, -HUGE_VAL, 0.0}, up[3] = {HUGE_VAL, HUGE_VAL, 0.0};
+            az.each_range([&](int tz, int z0, int z1) {
+                lo[2] = z0 - c[2];
+                up[2] = z1 - c[2];
+                lo[1] = lo[0] = -HUGE_VAL;
+                up[1] = up[0] = HUGE_VAL;
+                if (box_min_q(B.G, lo, up) > rg) return;
+                ay.each_range([&](int ty, int y0, int y1) {
+                    lo[1] = y0 - c[1];
+                    up[1] = y1 - c[1];
+                    lo[0] = -HUGE_VAL;
+                    up[0] = HUGE_VAL;
+                    if (box_min_q(B.G, lo, up) > rg) return;
+                    ax.each_range([&](int tx, int x0, int x1) {
+                        lo[0] = x0 - c[0];
+                        up[0] = x1 - c[0];
+                        if (box_min_q(B.G, lo, up) > rg) return;
+                        emit(tz, ty, tx);
+                    });
+                });
+            });
+            continue;
+        }
         az.each([&](int tz, int fz) {
             const double dz = fz * hz;
             if (!table && dz * dz > r2) return;
@@ -1548,9 +1664,7 @@ __global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, co
                 ax.each([&](int tx, int fx) {
                     const double dx = fx * hx;
                     if (!table && dz * dz + dy * dy + dx * dx > r2) return;
-                    const int tile = B.first + (tz * B.nt[1] + ty) * B.nt[0] + tx;
-                    if (pass == 0) atomicAdd(count + tile, 1);
-                    else items[atomicAdd(cursor + tile, 1ull)] = word;
+                    emit(tz, ty, tx);
                 });
             });
         });
@@ -1712,6 +1826,10 @@ int mixed_build(TaskSet &ts, std::string &err) {
         blv[l].nt[1] = lvl_first[l] >= 0 ? nty[l] : 0;
         blv[l].nt[2] = lvl_first[l] >= 0 ? ntz[l] : 0;
         blv[l].lz = ts.tile_lz[l] >= 0 ? ts.tile_lz[l] : kDefaultTileLz;
+        const LevelDev &lv = P.lv[l];
+        for (int a = 0; a < 3; a++)
+            for (int b = 0; b < 3; b++)
+                blv[l].G[a][b] = lv.dh[a][0] * lv.dh[b][0] + lv.dh[a][1] * lv.dh[b][1] + lv.dh[a][2] * lv.dh[b][2];
     }
     const int ntiles = (int)tiles.size();
     // blob layout: per task the record, then its coefficients
@@ -1826,8 +1944,12 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
     while (nto < ntiles && P.lv[M->h_tiles[nto].level].ortho) nto++;
     // Work units for the persistent queue: a tile with more items than ~1/64 of
     // an even share per SM is divided into units of consecutive items (their
-    // flushes add with FP64 atomics); units ordered by decreasing work within
-    // each group (orthorhombic, general).
+    // flushes add with FP64 atomics).  Within each group (orthorhombic, general)
+    // units run by decreasing work class (item counts within a factor 2^(1/4)
+    // share a class), and within a class in the tiles' raster order: the tiles in
+    // flight at one time then form a compact slab of the grid, so a pair's record,
+    // coefficients and moments stay in L2 between the neighbouring tiles that use
+    // them, while the short units still come last.
     const int64_t target = std::max<int64_t>(64, (nitems + 64LL * M->sms - 1) / std::max(1, 64 * M->sms));
     struct Unit {
         int tile;
@@ -1842,10 +1964,11 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
         for (int64_t u = 0; u < nu; u++)
             units.push_back(Unit{t, start[t] + n * u / nu, start[t] + n * (u + 1) / nu, nu > 1});
     }
+    auto work_class = [](const Unit &u) { return (int)std::floor(4.0 * std::log2((double)(u.it1 - u.it0))); };
     std::stable_sort(units.begin(), units.end(), [&](const Unit &a, const Unit &b) {
         const bool ga = a.tile >= nto, gb = b.tile >= nto;
         if (ga != gb) return !ga;
-        return a.it1 - a.it0 > b.it1 - b.it0;
+        return work_class(a) > work_class(b);
     });
     const int nunits = (int)units.size();
     int nuo = 0;
@@ -1910,6 +2033,9 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
     M->grid_ctas = std::max(1, std::min(nunits, M->sms * M->per_sm));
     return GPW_SUCCESS;
 }
+
+int64_t mixed_items(const TaskSet &ts) { return ts.mixed ? ts.mixed->nitems : 0; }
+int64_t mixed_units(const TaskSet &ts) { return ts.mixed ? ts.mixed->ntiles : 0; }
 
 void mixed_free(TaskSet &ts) {
     MixedState *M = ts.mixed;
