@@ -140,12 +140,14 @@ class Clocks:
 
 
 # ----------------------------------------------------------------------------
-# DRAM bytes (read + write) per (tile, pair) item of each tiled kernel:
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch on the 3,000-pair
-# sample of the 1M-pair workload (256^3), divided by that launch's items; a launch's
-# traffic is estimated as this times its items (the committed profile summaries give
-# the captures and their item counts).
-TRAFFIC_PER_ITEM = {"k_collocate_tiled": None, "k_integrate_tiled": None}
+# DRAM bytes (read + write) of one launch of each tiled kernel on the 1M-pair
+# workload (256^3, tile 32 x 16 x 8, 79,272,268 (tile, pair) items), from a
+# single-pass ncu capture of dram__bytes_read.sum + dram__bytes_write.sum with
+# gpu__time_duration.sum.  Other workloads scale it by their item count (an
+# estimate: the share of a pair's record and coefficients served by L2 depends
+# on the workload).
+TRAFFIC_1M = {"k_collocate_tiled": (8.695e9 + 0.201e9, 79_272_268),
+              "k_integrate_tiled": (9.227e9 + 2.802e9, 79_272_268)}
 
 
 def algorithmic_flops(wl) -> tuple:
@@ -268,7 +270,10 @@ def reference_arm(args):
     value = float(np.median(vals))
     base["value"] = value
     line = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * wl.ntasks / value, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * wl.ntasks / value,
+            "ms_per_step_basis": "extrapolated: the whole workload at the pair rate of the timed sample "
+                                 "(each step times a bounded random sample of the pairs, cpu_baseline.sample)",
+            "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "impl": "reference", "config": {"workload": wl.name, "npairs": wl.ntasks, "precision": "fp64-cpu"},
             "cpu_baseline": base, "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0,
@@ -480,8 +485,9 @@ def main():
         kname = f"k_{dom}_tiled"
         roof = {"bound": "tensor", "kernel": kname, "achieved": achieved_tf, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved_tf / peak,
-                "traffic": TRAFFIC_PER_ITEM[kname] * items if TRAFFIC_PER_ITEM.get(kname) else None,
-                "traffic_basis": "bytes per item of the 3,000-pair capture x this launch's items",
+                "traffic": TRAFFIC_1M[kname][0] * items / TRAFFIC_1M[kname][1],
+                "traffic_basis": "measured on the 1M-pair workload (one-pass ncu capture), scaled by this "
+                                 "launch's (tile, pair) items",
                 "items_per_launch": items,
                 "peak_source": "bf16 sustained, MEASURED_PEAKS.json (of measured)",
                 "limiter": "FP32/integer instruction issue of the float-float stages, not the tensor pipe "
