@@ -397,13 +397,24 @@ struct IntVTile<true> {
     ff Vff[TX][MROWS];  // general cell: this tile's V (x-major: lanes read consecutive rows)
 };
 
+// Integrate's S[(z,y)][alpha] rows hold KP + 1 values (row stores by thread
+// (z,y) spread over the banks), and the block of rows of z starts 8 ceil(z/2)
+// values later still: the rows of z = 2w and 2w + 1, which the lanes of stage 2T
+// read side by side at the same alpha (16 x 34 words apart, one bank otherwise),
+// then lie 16 banks apart, and no block runs into the next.  T rows hold NPAIR_T
+// values (2 NPAIR_T = 16 mod 32 words) for the same reason.
+constexpr int kSRow = KP + 1;
+constexpr int NPAIR_T = NPAIR_MAX + (24 - NPAIR_MAX % 16) % 16;
+static_assert((2 * NPAIR_T) % 32 == 16, "T rows of adjacent z 16 banks apart");
+__device__ __forceinline__ int s_index(int row, int ly) { return row * kSRow + 8 * (((row >> ly) + 1) >> 1); }
+
 template <bool kGeneral>
 struct alignas(128) SmemInt : IntVTile<kGeneral> {
     union {
         __half A[2][NSL][MROWS * KP];  // masked V slices, K halves x in [0,16) and [16,32)
         struct {                       // after the MMAs have read A:
-            ff S[MROWS][KP + 1];       //   S[(z,y)][alpha], padded rows: conflict-free row stores
-            ff T[kMaxTZ][NPAIR_MAX];   //   stage-2 output T[z][(b,a)]
+            ff S[MROWS * kSRow + 8 * (kMaxTZ / 2)];  //   S[(z,y)][alpha] at s_index((z,y)) + alpha
+            ff T[kMaxTZ][NPAIR_T];     //   stage-2 output T[z][(b,a)]
         } st;
     };
     __half B[2][NSL][KP * KP];  // X' slices, N=16 (alpha) x K=16 per half
@@ -1306,6 +1317,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                 phase ^= 1u;
                 if (!ok) break;
                 const bool live = sm.rx0[m] <= sm.rx1[m];
+                ff *const srow = sm.st.S + s_index(m, sh.ly);
 #pragma unroll 1
                 for (int c = 0; c < KP / 8; c++) {
                     if (8 * c >= L) break;  // uniform: S columns alpha >= L are not read
@@ -1334,7 +1346,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                                 s = {__fmul_rn(t.hi, scl), __fmul_rn(t.lo, scl)};
                             }
                         }
-                        sm.st.S[m][a] = s;
+                        srow[a] = s;
                     }
                 }
                 tc::fence_before_sync();
@@ -1349,10 +1361,11 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                     const int q = t >> lzw, b = qbL[q];  // q = pair_index(L, b, a)
                     const int a = q - (b * L - (b * (b - 1)) / 2);
                     ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
+                    const ff *sz = sm.st.S + s_index(zz * TY, sh.ly) + a;  // rows (zz, y) at sz[y * kSRow]
 #pragma unroll 2
                     for (int yy = 0; yy < TY; yy += 2) {
-                        ff_acc_lazy(s0, sm.st.S[zz * TY + yy][a], cm.Y[b][yy]);
-                        ff_acc_lazy(s1, sm.st.S[zz * TY + yy + 1][a], cm.Y[b][yy + 1]);
+                        ff_acc_lazy(s0, sz[yy * kSRow], cm.Y[b][yy]);
+                        ff_acc_lazy(s1, sz[(yy + 1) * kSRow], cm.Y[b][yy + 1]);
                     }
                     sm.st.T[zz][q] = ff_add(s0, s1);
                 }
