@@ -408,6 +408,19 @@ constexpr int NPAIR_T = NPAIR_MAX + (24 - NPAIR_MAX % 16) % 16;
 static_assert((2 * NPAIR_T) % 32 == 16, "T rows of adjacent z 16 banks apart");
 __device__ __forceinline__ int s_index(int row, int ly) { return row * kSRow + 8 * (((row >> ly) + 1) >> 1); }
 
+// Integrate's B operand (N = 16 alpha x K = 16 x per half, per slice): core
+// matrices 160 bytes apart along K and 288 along N, the second K half 64 bytes
+// further on.  Warp 0 stores one alpha row at a time, lane (h, k) the 2-byte
+// element (alpha, k) of half h: the four groups of 8 lanes (h, k / 8) then fill
+// four disjoint sets of 4 banks (the dense layout, 128 and 2048 bytes apart, put
+// all four into the same banks).
+constexpr int kBLbo = 160, kBSbo = 288, kBPlane = 576;       // bytes
+constexpr int kBHalf = NSL * kBPlane + 64;                   // bytes from half 0 to half 1
+__host__ __device__ constexpr int b_off(int row, int k) {    // bytes within a plane
+    return (row >> 3) * kBSbo + (k >> 3) * kBLbo + (row & 7) * 16 + (k & 7) * 2;
+}
+static_assert(b_off(15, 15) + 2 <= kBPlane && kBPlane % 16 == 0 && kBHalf % 16 == 0, "B planes");
+
 template <bool kGeneral>
 struct alignas(128) SmemInt : IntVTile<kGeneral> {
     union {
@@ -417,7 +430,7 @@ struct alignas(128) SmemInt : IntVTile<kGeneral> {
             ff T[kMaxTZ][NPAIR_T];     //   stage-2 output T[z][(b,a)]
         } st;
     };
-    __half B[2][NSL][KP * KP];  // X' slices, N=16 (alpha) x K=16 per half
+    alignas(16) unsigned char B[2 * kBHalf];  // X' slices: plane (h, q) at h kBHalf + q kBPlane
     int vmr[MROWS];  // general cell: each row's exponent of V E in the current image
     int gexp[KP];
     signed char rx0[MROWS], rx1[MROWS];  // each row's cube x range in the current image
@@ -1135,7 +1148,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
     }
     // B rows alpha >= L are never written: start them finite (zero)
     for (int t = tid; t < (int)(sizeof(sm.B) / sizeof(uint4)); t += NTHR)
-        reinterpret_cast<uint4 *>(&sm.B[0][0][0])[t] = make_uint4(0u, 0u, 0u, 0u);
+        reinterpret_cast<uint4 *>(sm.B)[t] = make_uint4(0u, 0u, 0u, 0u);
     for (;;) {
         if (tid == 0) cm.tile = atomicAdd(A.queue, 1);
         __syncthreads();
@@ -1240,9 +1253,10 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                         const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
                         float sl[NSL];
                         slice_scaled(xv[a], sc, sl);
-                        const int o = umma_off(a, tid & 15) >> 1, h = tid >> 4;
+                        unsigned char *const bp = sm.B + (tid >> 4) * kBHalf + b_off(a, tid & 15);
 #pragma unroll
-                        for (int q = 0; q < NSL; q++) sm.B[h][q][o] = __float2half_rn(sl[q]);
+                        for (int q = 0; q < NSL; q++)
+                            *reinterpret_cast<__half *>(bp + q * kBPlane) = __float2half_rn(sl[q]);
                     }
                 } else if (warp == 1) {
                     if constexpr (!kGeneral) bar_arrive1(NTHR);
@@ -1295,7 +1309,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                     for (int h = 0; h < 2; h++)
                         for (int q = 0; q < NSL; q++) {
                             a_[h][q] = tc::desc_kmajor(sm.A[h][q], 128, 256);
-                            b_[h][q] = tc::desc_kmajor(sm.B[h][q], 128, 256);
+                            b_[h][q] = tc::desc_kmajor(sm.B + h * kBHalf + q * kBPlane, kBLbo, kBSbo);
                         }
                     // D2 per K half (exact: 16 products each); diagonals 3.. over both halves
                     tc::mma_f16(cm.tmem + 0, a_[0][0], b_[0][0], idesc, 0);
