@@ -559,41 +559,59 @@ __device__ __forceinline__ void pair_images(TileCommon &sm, const TPair &p, cons
 // re-expansion column); zero outside the cube box, outside the valid tile extent
 // and for k >= L.
 //
-// Y and Z: entries 0 .. TY-1 and TY .. TY+TZ-1 over the lanes of warp 1, into
-// shared memory, one code path with runtime loops.
-__device__ void build_yz(TileCommon &sm, const TPair &p, const ImgState &q, const LevelDev &lv, const TileDesc &td) {
-    const TileShape sh(td.lz);
-#pragma unroll 1
-    for (int ent = (int)threadIdx.x - 32; ent < sh.TY + sh.TZ; ent += 32) {
+// One entry per lane: warp 0 entry x of the x column (kept in registers), warp 1
+// entry ent of the y table (ent < TY) or of the z table.  In collocate both warps
+// run one loop over entries, so that the kernel holds a single copy of the
+// float-float exponential, its largest inlined function: collocate is limited by
+// instruction fetch, and this alone took it from 995 to 926 ms per launch on the
+// 1M-pair workload.
+struct TabEntry {
+    ff t, e;    // t = g h - off and exp(-zetp t^2) (zero outside)
+    int d, i;   // axis and tile-local index
+    bool in;    // inside the cube box and the tile's valid extent
+};
+__device__ __forceinline__ TabEntry tab_entry(const TPair &p, const ImgState &q, const LevelDev &lv,
+                                              const TileDesc &td, const TileShape &sh, int warp, int ent) {
+    TabEntry r;
+    int T;
+    if (warp == 0) {
+        r.d = 0;
+        r.i = ent;
+        T = TX;
+    } else {
         const bool isy = ent < sh.TY;
-        const int d = isy ? 1 : 2, i = isy ? ent : ent - sh.TY, T = isy ? sh.TY : sh.TZ;
-        const int stride = isy ? kMaxTY + 1 : kMaxTZ + 1;
-        ff *col = isy ? &sm.Y[0][i] : &sm.Z[0][i];
-        const int g = q.o[d] + i;
-        const bool in = i < min(T, lv.ngrid[d] - td.t[d] * T) && g >= p.lb[d] && g <= p.hi[d];
-        const int L = in ? p.L : 0;
-        if (in) {
-            const ff t = ff_add(ff_mul_f(p.h[d], (float)g), ff{-p.off[d].hi, -p.off[d].lo});
-            ff e = ff_exp(ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo}));
-#pragma unroll 1
-            for (int k = 0; k < L; k++) {
-                col[k * stride] = e;
-                e = ff_mul(e, t);
-            }
-        }
-#pragma unroll 1
-        for (int k = L; k < kNPow; k++) col[k * stride] = ff{0.0f, 0.0f};
+        r.d = isy ? 1 : 2;
+        r.i = isy ? ent : ent - sh.TY;
+        T = isy ? sh.TY : sh.TZ;
     }
+    const int g = q.o[r.d] + r.i;
+    r.in = r.i < min(T, lv.ngrid[r.d] - td.t[r.d] * T) && g >= p.lb[r.d] && g <= p.hi[r.d];
+    r.t = ff_add(ff_mul_f(p.h[r.d], (float)g), ff{-p.off[r.d].hi, -p.off[r.d].lo});
+    r.e = r.in ? ff_exp(ff_mul(ff_mul(r.t, r.t), ff{-p.zetp.hi, -p.zetp.lo})) : ff{0.0f, 0.0f};
+    return r;
 }
-
-// X: column x in registers of one thread (warp 0, x = lane), xv[k] for k < kNPow
-__device__ __forceinline__ void x_column(const TPair &p, const ImgState &q, int x, bool recentre, ff *xv) {
+// warp 1: one y or z entry into shared memory
+__device__ __forceinline__ void yz_fill(TileCommon &sm, const TPair &p, const TabEntry &te) {
+    ff *col = te.d == 1 ? &sm.Y[0][te.i] : &sm.Z[0][te.i];
+    const int stride = te.d == 1 ? kMaxTY + 1 : kMaxTZ + 1;
+    const int L = te.in ? p.L : 0;
+    ff e = te.e;
+#pragma unroll 1
+    for (int k = 0; k < L; k++) {
+        col[k * stride] = e;
+        e = ff_mul(e, te.t);
+    }
+#pragma unroll 1
+    for (int k = L; k < kNPow; k++) col[k * stride] = ff{0.0f, 0.0f};
+}
+// warp 0: the x column of entry x in registers, xv[k] for k < kNPow
+__device__ __forceinline__ void x_powers(const TPair &p, const ImgState &q, const TabEntry &te, int x, bool recentre,
+                                         ff *xv) {
 #pragma unroll
     for (int k = 0; k < kNPow; k++) xv[k] = ff{0.0f, 0.0f};
-    if (x < q.gx0 || x > q.gx1) return;
-    const ff t = ff_add(ff_mul_f(p.h[0], (float)(q.o[0] + x)), ff{-p.off[0].hi, -p.off[0].lo});
-    ff e = ff_exp(ff_mul(ff_mul(t, t), ff{-p.zetp.hi, -p.zetp.lo}));
-    const ff u = recentre ? ff_mul_f(p.h[0], ldexpf((float)(x - q.ic), -q.sb)) : t;
+    if (!te.in) return;
+    ff e = te.e;
+    const ff u = recentre ? ff_mul_f(p.h[0], ldexpf((float)(x - q.ic), -q.sb)) : te.t;
 #pragma unroll
     for (int k = 0; k < kNPow; k++) {
         if (k >= p.L) break;
@@ -981,19 +999,25 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                 if (Q.gx0 > Q.gx1) continue;  // uniform: no x overlap
                 // warp 0: X column (lane x) and its B slices, scaled by 2^(SLB - fx); warp 1:
                 // Y and Z tables; warps 2-3: re-expansion of the coefficients
-                if (warp == 0) {
-                    ff xv[kNPow];
-                    x_column(P, Q, tid, true, xv);
-                    float mx = 0.0f;
+                if (warp < 2) {
+#pragma unroll 1
+                    for (int ent = tid & 31; ent < (warp == 0 ? TX : TY + TZ); ent += 32) {
+                        const TabEntry te = tab_entry(P, Q, lv, td, sh, warp, ent);
+                        if (warp == 0) {
+                            ff xv[kNPow];
+                            x_powers(P, Q, te, ent, true, xv);
+                            float mx = 0.0f;
 #pragma unroll
-                    for (int k = 0; k < kNPow; k++) mx = fmaxf(mx, fabsf(xv[k].hi));
-                    const int e = exp_of(mx);
-                    sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
-                    const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
-                    // K slots beyond L may hold an earlier pair's slices: rewritten as zeros
-                    slice_row16(xv, sc, max(L, cm.kmax), L, sm.B[0], TX * KP, tid);
-                } else if (warp == 1) {
-                    build_yz(cm, P, Q, lv, td);
+                            for (int k = 0; k < kNPow; k++) mx = fmaxf(mx, fabsf(xv[k].hi));
+                            const int e = exp_of(mx);
+                            sm.cs[tid] = e == kZeroExp ? 0.0f : pow2i(e);
+                            const float sc = e == kZeroExp ? 0.0f : pow2i(SLB - e);
+                            // K slots beyond L may hold an earlier pair's slices: rewritten as zeros
+                            slice_row16(xv, sc, max(L, cm.kmax), L, sm.B[0], TX * KP, tid);
+                        } else {
+                            yz_fill(cm, P, te);
+                        }
+                    }
                 } else {
                     // slab starts zs[g] = packed index of (g, 0, 0), then the re-expansion
                     if (tid - 64 <= kNPow) sm.zs[tid - 64] = tid - 64 <= lp + 1 ? row_start(lp, tid - 64, 0) : 0;
@@ -1238,9 +1262,11 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                     if constexpr (!kGeneral) bar_arrive1(NTHR);
                     // X column (lane x) in registers, then B: row alpha = X[alpha][x] over x,
                     // scaled by 2^(SLB - gexp[alpha]) (maximum over the warp); rows alpha >= L
-                    // are left as they are (their output columns are not read)
+                    // are left as they are (their output columns are not read).  Unlike
+                    // collocate, integrate is not limited by instruction fetch: warps 0 and 1
+                    // keep separate table code.
                     ff xv[kNPow];
-                    x_column(P, Q, tid, false, xv);
+                    x_powers(P, Q, tab_entry(P, Q, lv, td, sh, 0, tid), tid, false, xv);
 #pragma unroll
                     for (int a = 0; a < kNPow; a++) {
                         if (a >= L) break;
@@ -1261,7 +1287,8 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                 } else if (warp == 1) {
                     if constexpr (!kGeneral) bar_arrive1(NTHR);
                     if (tid - 32 <= kNPow) sm.zs[tid - 32] = tid - 32 <= lp + 1 ? row_start(lp, tid - 32, 0) : 0;
-                    build_yz(cm, P, Q, lv, td);
+#pragma unroll 1
+                    for (int ent = tid - 32; ent < TY + TZ; ent += 32) yz_fill(cm, P, tab_entry(P, Q, lv, td, sh, 1, ent));
                 } else if constexpr (!kGeneral) {
                     bar_sync1(NTHR);
                     // A operand: V slices of rows u and u + 64 (the CTA's slot) masked to the rows' cube ranges,
