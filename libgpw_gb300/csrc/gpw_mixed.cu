@@ -653,6 +653,7 @@ __device__ void recentre_x(const PairBuf &pb, ff tc, ff *out, const float (*bin)
         const int a = r - (b * (qn + 1) - (b * (b - 1)) / 2), amax = lp - g - b;
         const int base = t - a;  // packed index of (g, b, 0)
         ff s = {0.0f, 0.0f};
+#pragma unroll 1
         for (int ap = amax; ap >= a; ap--) {
             const float2 c = pb.coef[base + ap];
             s = ff_fma(s, tc, ff_mul_f(ff{c.x, c.y}, bin[ap][a]));
@@ -876,6 +877,7 @@ __device__ __forceinline__ void stage1_cxy(SmemColl &sm, int L, int lp, const Ti
         const int k0 = b * (lp + 1) - (b * (b - 1)) / 2 + a;
         ff s0 = {0.0f, 0.0f}, s1 = {0.0f, 0.0f};
         int g = 0, bg = 0;
+#pragma unroll 1
         for (; g + 1 <= n; g += 2, bg += 2 * b) {
             s0 = ff_fma(sm.rc[sm.zs[g] - bg + k0], cm.Z[g][zz], s0);
             s1 = ff_fma(sm.rc[sm.zs[g + 1] - bg - b + k0], cm.Z[g + 1][zz], s1);
@@ -1135,12 +1137,19 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
             double *grid = A.grids.p[td.level];
             const int64_t row = ((int64_t)(td.t[2] * TZ + z) * lv.ngrid[1] + (td.t[1] * TY + y)) * lv.ngrid[0] +
                                 td.t[0] * TX;
+            // 8 points per iteration, acc_hi rotated by 8 as in the readout (compact code)
+#pragma unroll 1
+            for (int c = 0; c < TX / 8; c++) {
 #pragma unroll
-            for (int x = 0; x < TX; x++) {
-                if (x >= ext_x) continue;
-                const double v = (double)acc_hi[x] + (double)acc_lo[x];
-                if (td.split) atomicAdd(grid + row + x, v);  // other work units add to the same tile
-                else grid[row + x] += v;
+                for (int i = 0; i < 8; i++) {
+                    const int x = 8 * c + i;
+                    if (x >= ext_x) continue;
+                    const double v = (double)acc_hi[i] + (double)acc_lo[x];
+                    if (td.split) atomicAdd(grid + row + x, v);  // other work units add to the same tile
+                    else grid[row + x] += v;
+                }
+#pragma unroll
+                for (int i = 0; i < TX - 8; i++) acc_hi[i] = acc_hi[i + 8];
             }
         }
         __syncthreads();
