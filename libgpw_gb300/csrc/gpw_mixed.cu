@@ -1311,13 +1311,17 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                             x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));  // bits x0..x1
                         if (M == 0u && zero_row[rr]) continue;
                         zero_row[rr] = M == 0u;
-                        uint4 val[TX / 8][NSL];  // all loads of the row first (from the slot): latencies overlap
+                        // all loads of the row first (from the slot): latencies overlap; chunks of 8
+                        // x outside the row's range are not loaded (they are stored as zeros)
+                        uint4 val[TX / 8][NSL];
 #pragma unroll
                         for (int v = 0; v < TX / 8; v++)
 #pragma unroll
                             for (int q = 0; q < NSL; q++)
-                                val[v][q] = vslot[((v >> 1) * NSL + q) * (MROWS * KP / 8) + (r >> 3) * 16 +
-                                                  (v & 1) * 8 + (r & 7)];
+                                val[v][q] = ((M >> (8 * v)) & 0xFFu)
+                                                ? vslot[((v >> 1) * NSL + q) * (MROWS * KP / 8) + (r >> 3) * 16 +
+                                                        (v & 1) * 8 + (r & 7)]
+                                                : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                         for (int v = 0; v < TX / 8; v++) {
                             const uint32_t mv = M >> (8 * v);
