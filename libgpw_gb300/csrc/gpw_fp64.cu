@@ -160,7 +160,10 @@ int smem_ortho_fp64(const PairGeom &g, int extra) {
     return 8 * (L * L * L + L * (nx + ny + nz) + L * L + ny * L) + 8 * ny;
 }
 
-template <bool kAdj>
+// kAcc: the row accumulators of the adjoint, L <= kAcc (kNPow for integrate,
+// kNPowB for the backward pass's moments to degree lp + 2: more accumulators cost
+// the plain integrate registers and shuffles)
+template <bool kAdj, int kAcc = kNPow>
 __global__ void __launch_bounds__(256)
 k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__restrict__ levels,
              const int *__restrict__ table, const double *__restrict__ coef, double *__restrict__ mom,
@@ -234,9 +237,9 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
                 continue;
             }
             const int64_t rowbase = ((int64_t)k * lv.ngrid[1] + j) * lv.ngrid[0];
-            double acc[kNPowB];
+            double acc[kAcc];
 #pragma unroll
-            for (int lx = 0; lx < kNPowB; lx++) acc[lx] = 0.0;
+            for (int lx = 0; lx < kAcc; lx++) acc[lx] = 0.0;
             for (int ig = igmin + lane; ig <= 1 - igmin; ig += 32) {
                 const int i = axis_index(lv.periodic[0], g.cc[0], ig, g.lb[0], lv.lb_grid[0],
                                          lv.npts[0], lv.ngrid[0]);
@@ -252,14 +255,14 @@ k_ortho_fp64(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
                 } else {
                     const double v = grid[rowbase + i];
 #pragma unroll
-                    for (int lx = 0; lx < kNPowB; lx++)
+                    for (int lx = 0; lx < kAcc; lx++)
                         if (lx < L) acc[lx] += v * Xi[lx * nx];
                 }
             }
             if (kAdj) {
                 // warp-shuffle reduction of the row moments
 #pragma unroll
-                for (int lx = 0; lx < kNPowB; lx++) {
+                for (int lx = 0; lx < kAcc; lx++) {
                     double v = acc[lx];
                     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
                     acc[lx] = v;
@@ -630,6 +633,7 @@ static cudaError_t set_smem(const void *fn, int bytes) {
 cudaError_t fp64_kernel_attributes(int smem_max) {
     const void *fns[] = {(const void *)k_prep, (const void *)k_backtransform,
                          (const void *)k_ortho_fp64<false>, (const void *)k_ortho_fp64<true>,
+                         (const void *)k_ortho_fp64<true, kNPowB>,
                          (const void *)k_general_fp64<false>, (const void *)k_general_fp64<true>,
                          (const void *)k_general_ff<false>, (const void *)k_general_ff<true>};
     for (const void *fn : fns) {
@@ -657,10 +661,14 @@ static cudaError_t launch_fp64_impl(const TaskSet &ts, const GridPtrs &g, bool a
         cudaError_t e;
         ProfScope prof(ts, s);
         if (c.kind == 0) {
-            if (adj)
+            if (adj && extra)
+                k_ortho_fp64<true, kNPowB><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
+                                                                             ts.d_table, ts.d_coef, mom, g,
+                                                                             ts.d_status, extra);
+            else if (adj)
                 k_ortho_fp64<true><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
                                                                      ts.d_table, ts.d_coef, mom, g,
-                                                                     ts.d_status, extra);
+                                                                     ts.d_status, 0);
             else
                 k_ortho_fp64<false><<<c.count, 256, c.smem_bytes, s>>>(ts.d_geom, c.first, ts.plan->d_levels,
                                                                       ts.d_table, ts.d_coef, mom, g,
