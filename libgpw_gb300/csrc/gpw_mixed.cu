@@ -1668,11 +1668,14 @@ struct AxisRuns {
 // tile's nearest offsets <= radius; general cell, the least |r - rp|^2 over the
 // lattice-index box of the tile's offsets (box_min_q) <= radius^2, tested per z
 // run, then per (z, y) runs, then per tile.  Explicit cube lists are not culled.
-__global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, const LevelDev *__restrict__ levels,
-                            const BinLevel *__restrict__ bl, const int64_t *__restrict__ off16,
-                            const int *__restrict__ len16, int pass, int *count, unsigned long long *cursor,
-                            uint64_t *items) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nbin; k += (int64_t)gridDim.x * blockDim.x) {
+// kGen: the general-cell pairs [k0, k1) (the culling's box minimum needs registers
+// and stack that would slow the orthorhombic launch, kGen = false).
+template <bool kGen>
+__global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t k0, int64_t k1,
+                            const LevelDev *__restrict__ levels, const BinLevel *__restrict__ bl,
+                            const int64_t *__restrict__ off16, const int *__restrict__ len16, int pass, int *count,
+                            unsigned long long *cursor, uint64_t *items) {
+    for (int64_t k = k0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < k1; k += (int64_t)gridDim.x * blockDim.x) {
         const PairGeom &g = geoms[k];
         const LevelDev &lv = levels[g.level];
         const BinLevel B = bl[g.level];
@@ -1695,7 +1698,7 @@ __global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, co
             if (pass == 0) atomicAdd(count + tile, 1);
             else items[atomicAdd(cursor + tile, 1ull)] = word;
         };
-        if (!g.ortho) {
+        if constexpr (kGen) {
             // lattice-index offsets from the product centre: d_a = cc_a + gg - gp_a
             const double c[3] = {g.off[0] - g.cc[0], g.off[1] - g.cc[1], g.off[2] - g.cc[2]};
             const double rg = g.radius * g.radius * (1.0 + 1e-6) + 1e-12;
@@ -1720,8 +1723,7 @@ __global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, co
                     });
                 });
             });
-            continue;
-        }
+        } else {
         az.each([&](int tz, int fz) {
             const double dz = fz * hz;
             if (!table && dz * dz > r2) return;
@@ -1735,7 +1737,22 @@ __global__ void k_bin_pairs(const PairGeom *__restrict__ geoms, int64_t nbin, co
                 });
             });
         });
+        }
     }
+}
+
+// both kinds of pairs of a task set (orthorhombic first in the sorted order)
+static cudaError_t bin_pairs(const TaskSet &ts, const MixedState &M, int pass, int *count,
+                             unsigned long long *cursor, uint64_t *items) {
+    const Plan &P = *ts.plan;
+    auto blocks = [](int64_t n) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + 127) / 128, 8192)); };
+    if (M.northo > 0)
+        k_bin_pairs<false><<<blocks(M.northo), 128>>>(ts.d_geom, 0, M.northo, P.d_levels, M.d_bl, M.d_blob_off,
+                                                      M.d_blob_len, pass, count, cursor, items);
+    if (M.nbin > M.northo)
+        k_bin_pairs<true><<<blocks(M.nbin - M.northo), 128>>>(ts.d_geom, M.northo, M.nbin, P.d_levels, M.d_bl,
+                                                              M.d_blob_off, M.d_blob_len, pass, count, cursor, items);
+    return cudaGetLastError();
 }
 
 // The record (TPair) of every binned pair from its geometry, into its blob.
@@ -1995,11 +2012,7 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
         if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
     }
     if ((e = cudaMemset(M->d_count, 0, sizeof(int) * (size_t)std::max(ntiles, 1))) != cudaSuccess) return fail(e);
-    if (nbin > 0) {
-        k_bin_pairs<<<nblk, 128>>>(ts.d_geom, nbin, P.d_levels, M->d_bl, M->d_blob_off, M->d_blob_len, 0,
-                                   M->d_count, nullptr, nullptr);
-        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
-    }
+    if (nbin > 0 && (e = bin_pairs(ts, *M, 0, M->d_count, nullptr, nullptr)) != cudaSuccess) return fail(e);
     std::vector<int> count((size_t)std::max(ntiles, 1), 0);
     if ((e = cudaMemcpy(count.data(), M->d_count, sizeof(int) * count.size(), cudaMemcpyDeviceToHost)) != cudaSuccess)
         return fail(e);
@@ -2080,11 +2093,7 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
     if ((e = cudaMemcpy(M->d_cursor, cur.data(), sizeof(unsigned long long) * cur.size(), cudaMemcpyHostToDevice)) !=
         cudaSuccess)
         return fail(e);
-    if (nbin > 0) {
-        k_bin_pairs<<<nblk, 128>>>(ts.d_geom, nbin, P.d_levels, M->d_bl, M->d_blob_off, M->d_blob_len, 1,
-                                   nullptr, M->d_cursor, M->d_items);
-        if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
-    }
+    if (nbin > 0 && (e = bin_pairs(ts, *M, 1, nullptr, M->d_cursor, M->d_items)) != cudaSuccess) return fail(e);
     if (nitems) {
         // image overflows are reported by the tiled kernels when they run (a plain
         // FP64 call on this task set must not see them)
