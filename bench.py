@@ -146,8 +146,8 @@ class Clocks:
 # gpu__time_duration.sum.  Other workloads scale it by their item count (an
 # estimate: the share of a pair's record and coefficients served by L2 depends
 # on the workload).
-TRAFFIC_1M = {"k_collocate_tiled": (8.695e9 + 0.201e9, 79_272_268),
-              "k_integrate_tiled": (9.227e9 + 2.802e9, 79_272_268)}
+TRAFFIC_1M = {"k_collocate_tiled": (9.028e9 + 0.193e9, 79_272_268),
+              "k_integrate_tiled": (9.510e9 + 2.966e9, 79_272_268)}
 
 
 def algorithmic_flops(wl) -> tuple:
