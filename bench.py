@@ -214,9 +214,18 @@ def cpu_baseline(wl, seconds: float, seed: int = 0) -> dict:
         if elapsed >= seconds * 0.4 or n >= wl.ntasks:
             break
         n = int(min(wl.ntasks, max(2 * n, n * seconds * 0.6 / max(elapsed, 1e-3))))
+    # the same on one core, on a sample of about the same duration
+    idx1 = idx[: max(4, len(idx) // threads)]
+    sw1 = subsample(wl, idx1)
+    t0 = time.perf_counter()
+    O.batch(sw1, nthreads=1)
+    O.batch(sw1, V=V, nthreads=1)
+    el1 = time.perf_counter() - t0
     return {"value": len(idx) / elapsed, "unit": "pairs/s", "cores": threads, "kind": kind,
+            "value_1core": len(idx1) / el1,
             "sample": f"{len(idx)} random pairs of the {wl.ntasks}-pair workload, collocate+integrate FP64, "
-                      f"{threads} threads with private grids, {elapsed:.1f} s"}
+                      f"{threads} threads with private grids, {elapsed:.1f} s; 1 core: the first {len(idx1)} "
+                      f"of them, {el1:.1f} s"}
 
 
 def fp64_gemm_rate(dev) -> float:
