@@ -72,3 +72,35 @@ def test_autotune_picks_a_candidate(tmp_path):
     g64 = run_collocate(wl, "fp64", ts=ts, plan=plan)[0]
     gmx = run_collocate(wl, "mixed", ts=ts, plan=plan)[0]
     assert rel_l2(gmx, g64) <= TOL
+
+
+def test_bins_follow_the_tile_shapes():
+    """gpw_taskset_bins: every pair meets at least one tile; smaller tiles (tz = 4
+    on one level is 32 x 32 x 4) give a different item count; a general-cell
+    level left untiled (tz = 0) has no items, and tiled it has at most as many
+    as the tiles its pairs' index boxes can span (an upper bound; the culling
+    itself is checked by the parity tests on the same distribution)."""
+    wl = T.config(5, npairs=400, seed=23)
+    plan = capi.Plan(wl.levels)
+    ts = capi.TaskSet.from_workload(plan, wl)
+    ts.set_tiles([8])
+    items8, units8 = ts.bins()
+    assert items8 >= wl.ntasks and units8 >= 1
+    ts.set_tiles([4])
+    items4, _ = ts.bins()
+    assert items4 >= wl.ntasks and items4 != items8
+
+    wg = T.config(3, npairs=200, seed=24)
+    plan_g = capi.Plan(wg.levels)
+    ts_g = capi.TaskSet.from_workload(plan_g, wg)
+    ts_g.set_tiles([0])
+    assert ts_g.bins() == (0, 0)
+    ts_g.set_tiles([8])
+    items_g, units_g = ts_g.bins()
+    assert items_g >= wg.ntasks and units_g >= 1
+    # tiles of 32 x 16 x 8 that each index box spans, without culling
+    g = wg.levels[0]
+    span = 2 * np.ceil(wg.tasks["radius"][:, None] * np.abs(np.asarray(g["dh_inv"])).sum(axis=0)[None, :]) + 1
+    n = np.asarray(g["npts"], dtype=np.float64)
+    boxes = np.prod(np.minimum(np.ceil(span / np.array([32.0, 16.0, 8.0])) + 1, n / np.array([32.0, 16.0, 8.0])), axis=1)
+    assert items_g <= boxes.sum()
