@@ -610,13 +610,27 @@ __device__ __forceinline__ void x_powers(const TPair &p, const ImgState &q, cons
 #pragma unroll
     for (int k = 0; k < kNPow; k++) xv[k] = ff{0.0f, 0.0f};
     if (!te.in) return;
-    ff e = te.e;
-    const ff u = recentre ? ff_mul_f(p.h[0], ldexpf((float)(x - q.ic), -q.sb)) : te.t;
+    if (recentre) {  // collocate: one chain (its code size matters more than this latency)
+        ff e = te.e;
+        const ff u = ff_mul_f(p.h[0], ldexpf((float)(x - q.ic), -q.sb));
 #pragma unroll
-    for (int k = 0; k < kNPow; k++) {
+        for (int k = 0; k < kNPow; k++) {
+            if (k >= p.L) break;
+            xv[k] = e;
+            e = ff_mul(e, u);
+        }
+        return;
+    }
+    // integrate: even and odd powers of t as two independent chains in t^2
+    const ff u2 = ff_mul(te.t, te.t);
+    ff e0 = te.e, e1 = ff_mul(te.e, te.t);
+#pragma unroll
+    for (int k = 0; k < kNPow; k += 2) {
         if (k >= p.L) break;
-        xv[k] = e;
-        e = ff_mul(e, u);
+        xv[k] = e0;
+        if (k + 1 < kNPow && k + 1 < p.L) xv[k + 1] = e1;
+        e0 = ff_mul(e0, u2);
+        e1 = ff_mul(e1, u2);
     }
 }
 
