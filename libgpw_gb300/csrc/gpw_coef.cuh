@@ -169,6 +169,28 @@ __device__ inline double local_entry(const PairGeom &g, int func, const double *
 // P(b', a') of the local block of function `func` (gpw_function).
 __device__ inline void fill_local_block(CoefWs &w, const PairGeom &g, int func, const double *pab) {
     const int n = w.d.n_P();
+    if (func == GPW_FUNC_AB) {
+        // rho: the local block is the density block, in the same coset order, and
+        // zero below the pair's lowest shells; kU independent loads per thread are
+        // in flight together
+        constexpr int kU = 8;
+        const int nla = w.d.nla, a_lo = ncoset(g.la0_min - 1), b_lo = ncoset(g.lb0_min - 1);
+        for (int t0 = threadIdx.x; t0 < n; t0 += kU * blockDim.x) {
+            double v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const int t = t0 + u * blockDim.x;
+                const int jco = t / nla, ico = t - jco * nla;
+                v[u] = (t < n && ico >= a_lo && jco >= b_lo) ? __ldg(&pab[block_index(g, jco, ico)]) : 0.0;
+            }
+#pragma unroll
+            for (int u = 0; u < kU; u++) {
+                const int t = t0 + u * blockDim.x;
+                if (t < n) w.P[t] = v[u];
+            }
+        }
+        return;
+    }
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
         const int jco = t / w.d.nla, ico = t % w.d.nla;
         int a[3], b[3];
@@ -179,6 +201,10 @@ __device__ inline void fill_local_block(CoefWs &w, const PairGeom &g, int func, 
 }
 
 // c (packed, prefactor included) from P.  Writes packed coefficients to `out`.
+// Products with a structurally zero factor are not formed: a lattice power lx of
+// T1[(lya,lza)][(lyb,lzb)] is zero beyond (A-lya-lza) + (B-lyb-lzb), the largest
+// lxa + lxb of the block, so T2[lza][lzb][ly][lx] is zero for lx + ly beyond
+// (A-lza) + (B-lzb); the loop bounds below skip those terms.
 __device__ inline void forward_coef(CoefWs &w, const PairGeom &g, double *out) {
     const CoefDims &d = w.d;
     const int L = d.L;
@@ -207,12 +233,13 @@ __device__ inline void forward_coef(CoefWs &w, const PairGeom &g, double *out) {
         const int ly = (t / L) % L;
         const int lzb = (t / (L * L)) % (d.B + 1);
         const int lza = t / (L * L * (d.B + 1));
+        const int cap = d.A + d.B - lza - lzb - lx;  // ly <= lya + lyb <= cap
         double s = 0.0;
-        for (int lya = 0; lya <= d.A - lza; lya++)
-            for (int lyb = 0; lyb <= d.B - lzb; lyb++) {
-                if (ly > lya + lyb) continue;
+        for (int lya = 0; lya <= d.A - lza; lya++) {
+            const int b0 = max(ly - lya, 0), b1 = min(d.B - lzb, cap - lya);
+            for (int lyb = b0; lyb <= b1; lyb++)
                 s += w.T1[(tri(lya, lza) * d.nb2 + tri(lyb, lzb)) * L + lx] * w.AL(1, lya, lyb, ly);
-            }
+        }
         w.T2[t] = s;
     }
     __syncthreads();
@@ -221,27 +248,43 @@ __device__ inline void forward_coef(CoefWs &w, const PairGeom &g, double *out) {
     for (int t = threadIdx.x; t < L * L * L; t += blockDim.x) {
         const int lx = t % L, ly = (t / L) % L, lz = t / (L * L);
         if (lx + ly + lz > lp) continue;
+        const int cap = d.A + d.B - lx - ly;  // lz <= lza + lzb <= cap
         double s = 0.0;
-        for (int lza = 0; lza <= d.A; lza++)
-            for (int lzb = 0; lzb <= d.B; lzb++) {
-                if (lz > lza + lzb) continue;
+        for (int lza = 0; lza <= d.A; lza++) {
+            const int b0 = max(lz - lza, 0), b1 = min(d.B, cap - lza);
+            for (int lzb = b0; lzb <= b1; lzb++)
                 s += w.T2[((lza * (d.B + 1) + lzb) * L + ly) * L + lx] * w.AL(2, lza, lzb, lz);
-            }
+        }
         out[pidx(lp, lz, ly, lx)] = g.prefactor * s;
     }
 }
 
-// Adjoint: given moments W (packed like c), accumulate into hab.
+// Cartesian indices of the local shells (la, lb <= kMaxL + 1 after the shift of
+// the derivative functions)
+constexpr int kNcoLocal = ((kMaxL + 2) * (kMaxL + 3) * (kMaxL + 4)) / 6;
+
+// Adjoint: given moments W (packed like c), accumulate into hab.  Only the
+// entries the next stage reads are formed: X^T reads T1[(lya,lza)][(lyb,lzb)][lx]
+// for lx <= lxa + lxb <= (A-lya-lza) + (B-lyb-lzb), so Y^T reads T2[lza][lzb][ly][lx]
+// only for lx + ly <= (A-lza) + (B-lzb).
 __device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int func, const double *W,
                                     double *hab) {
     const CoefDims &d = w.d;
     const int L = d.L, lp = g.lp;
+    // coset index -> lx | ly << 4 | lz << 8, read after the next barrier
+    __shared__ int s_co[kNcoLocal];
+    for (int i = threadIdx.x; i < max(d.nla, d.nlb); i += blockDim.x) {
+        int x, y, z;
+        coset_decode(i, x, y, z);
+        s_co[i] = x | (y << 4) | (z << 8);
+    }
     // Z^T: T2[lza][lzb][ly][lx] = sum_lz al_z[lza][lzb][lz] W[lz][ly][lx]
     for (int t = threadIdx.x; t < d.n_T2(); t += blockDim.x) {
         const int lx = t % L;
         const int ly = (t / L) % L;
         const int lzb = (t / (L * L)) % (d.B + 1);
         const int lza = t / (L * L * (d.B + 1));
+        if (lx + ly > d.A + d.B - lza - lzb) continue;
         double s = 0.0;
         for (int lz = 0; lz <= lza + lzb && lz + ly + lx <= lp; lz++)
             s += w.AL(2, lza, lzb, lz) * W[pidx(lp, lz, ly, lx)];
@@ -256,6 +299,7 @@ __device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int func, cons
         int lya, lza, lyb, lzb;
         tri_decode(ta, lya, lza);
         tri_decode(tb, lyb, lzb);
+        if (lx > (d.A - lya - lza) + (d.B - lyb - lzb)) continue;
         double s = 0.0;
         for (int ly = 0; ly <= lya + lyb; ly++)
             s += w.AL(1, lya, lyb, ly) * w.T2[((lza * (d.B + 1) + lzb) * L + ly) * L + lx];
@@ -264,10 +308,9 @@ __device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int func, cons
     __syncthreads();
     // X^T: P[b][a] = pref * sum_lx al_x[lxa][lxb][lx] T1[(lya,lza)][(lyb,lzb)][lx]
     for (int t = threadIdx.x; t < d.n_P(); t += blockDim.x) {
-        const int jco = t / d.nla, ico = t % d.nla;
-        int a[3], b[3];
-        coset_decode(ico, a[0], a[1], a[2]);
-        coset_decode(jco, b[0], b[1], b[2]);
+        const int jco = t / d.nla, ico = t - jco * d.nla;
+        const int ca = s_co[ico], cb = s_co[jco];
+        const int a[3] = {ca & 15, (ca >> 4) & 15, ca >> 8}, b[3] = {cb & 15, (cb >> 4) & 15, cb >> 8};
         const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
         double s = 0.0;
         if (la >= g.la_min && la <= g.la_max && lb >= g.lb_min && lb <= g.lb_max) {
@@ -280,20 +323,26 @@ __device__ inline void adjoint_coef(CoefWs &w, const PairGeom &g, int func, cons
     __syncthreads();
     // block map transposed, into hab (pairs may share hab entries: atomics)
     const int na0 = ncoset(g.la0_max), nb0 = ncoset(g.lb0_max);
+    if (func == GPW_FUNC_AB) {
+        // rho: the same coset order, the pair's shells only
+        const int a_lo = ncoset(g.la0_min - 1), b_lo = ncoset(g.lb0_min - 1);
+        for (int t = threadIdx.x; t < na0 * nb0; t += blockDim.x) {
+            const int jco = t / na0, ico = t - jco * na0;
+            if (ico >= a_lo && jco >= b_lo) atomicAdd(&hab[block_index(g, jco, ico)], w.P[jco * d.nla + ico]);
+        }
+        return;
+    }
     for (int t = threadIdx.x; t < na0 * nb0; t += blockDim.x) {
-        const int jco = t / na0, ico = t % na0;
-        int a[3], b[3];
-        coset_decode(ico, a[0], a[1], a[2]);
-        coset_decode(jco, b[0], b[1], b[2]);
+        const int jco = t / na0, ico = t - jco * na0;
+        const int ca = s_co[ico], cb = s_co[jco];
+        const int a[3] = {ca & 15, (ca >> 4) & 15, ca >> 8}, b[3] = {cb & 15, (cb >> 4) & 15, cb >> 8};
         const int la = a[0] + a[1] + a[2], lb = b[0] + b[1] + b[2];
         if (la < g.la0_min || la > g.la0_max || lb < g.lb0_min || lb > g.lb0_max) continue;
         double s = 0.0;
         auto Pl = [&](const int at[3], const int bt[3]) {
             return w.P[coset(bt[0], bt[1], bt[2]) * d.nla + coset(at[0], at[1], at[2])];
         };
-        if (func == GPW_FUNC_AB) {
-            s = w.P[jco * d.nla + ico];
-        } else if (func >= GPW_FUNC_ADBMDAB_X) {
+        if (func >= GPW_FUNC_ADBMDAB_X) {
             // the transpose of local_entry: source (a, b) feeds (a, b - e), (a, b + e),
             // (a - e, b) and (a + e, b)
             const int dd = func - GPW_FUNC_ADBMDAB_X;

@@ -52,7 +52,7 @@ __global__ void k_prep(const PairGeom *__restrict__ geoms, const LevelDev *__res
                        const double *__restrict__ tmat, int tau, const double *__restrict__ pab,
                        double *__restrict__ coef) {
     extern __shared__ double sm[];
-    const PairGeom g = geoms[blockIdx.x];
+    const PairGeom &g = geoms[blockIdx.x];  // read in place (L1), not copied per thread
     CoefWs w;
     w.carve(sm, g.la_max, g.lb_max);
     fill_alpha(w, g);
@@ -110,7 +110,7 @@ __global__ void k_backtransform(const PairGeom *__restrict__ geoms, const LevelD
                                 const double *__restrict__ tmat, int tau,
                                 const double *__restrict__ mom, double *__restrict__ hab) {
     extern __shared__ double sm[];
-    const PairGeom g = geoms[blockIdx.x];
+    const PairGeom &g = geoms[blockIdx.x];  // read in place (L1), not copied per thread
     CoefWs w;
     w.carve(sm, g.la_max, g.lb_max);
     fill_alpha(w, g);
@@ -624,8 +624,12 @@ k_general_ff(const PairGeom *__restrict__ geoms, int first, const LevelDev *__re
 }
 
 // ---------------------------------------------------------------------------
+// bytes: the CTA's whole shared memory; a kernel's static shared arrays come out of it
 static cudaError_t set_smem(const void *fn, int bytes) {
-    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncAttributes a;
+    cudaError_t e = cudaFuncGetAttributes(&a, fn);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes - (int)a.sharedSizeBytes);
 }
 
 // Opt every dynamic-shared-memory kernel of this file into the device maximum once,
