@@ -1085,59 +1085,64 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     // bits x0..x1 of the row: the points of this pair's sphere on the row
                     const uint32_t rmask =
                         x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));
-                    // one chunk of 8 x per iteration (a compact loop body: instruction fetch is
-                    // a stall of this kernel); acc_hi[0..7] always holds the current chunk's
-                    // sums, rotated by 8 after each chunk (four rotations restore the order)
+                    // two chunks of 8 x per iteration (a compact loop body: instruction fetch is
+                    // a stall of this kernel); acc_hi[0..15] always holds the current chunks'
+                    // sums, rotated by 16 after each iteration (two rotations restore the order)
 #pragma unroll 1
-                    for (int c = 0; c < TX / 8; c++) {
-                        const uint32_t mc = rmask >> (8 * c);
-                        if (__any_sync(0xffffffffu, (mc & 0xFFu) != 0u)) {
-                            uint32_t r2[8], r3[8], r4[8], r5[8];
-                            const float4 csa = reinterpret_cast<const float4 *>(sm.cs)[2 * c];
-                            const float4 csb = reinterpret_cast<const float4 *>(sm.cs)[2 * c + 1];
-                            const float csv[8] = {csa.x, csa.y, csa.z, csa.w, csb.x, csb.y, csb.z, csb.w};
-                            tc::tmem_ld8(tbase + 8 * c, r2);
-                            tc::tmem_ld8(tbase + 32 + 8 * c, r3);
-                            tc::tmem_ld8(tbase + 64 + 8 * c, r4);
-                            tc::tmem_ld8(tbase + 96 + 8 * c, r5);
-                            tc::tmem_wait_ld32(r2, r3, r4, r5);
+                    for (int c2 = 0; c2 < TX / 16; c2++) {
 #pragma unroll
-                            for (int i = 0; i < 8; i++) {
-                                const int x = 8 * c + i;
-                                const bool in = (mc >> i) & 1u;  // straight-line code: selects, no branches
-                                // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
-                                // lo the exact remainder (fast two-sum), then an exact two-sum into
-                                // acc_hi: acc_lo then only gathers rounding errors and remainders,
-                                // so it stays ~2^-24 below acc_hi however many pairs a point sees
-                                const float d2 = __uint_as_float(r2[i]);
-                                const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
-                                                   __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
-                                                             __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
-                                float scl = __fmul_rn(rs, csv[i]);
-                                const float h0 = __fadd_rn(d2, corr);
-                                float hi = __fmul_rn(h0, scl);
-                                float rem = __fsub_rn(corr, __fsub_rn(h0, d2));  // lo = rem scl exactly
-                                if constexpr (kGeneral) {
-                                    if (x > x0) ecur = ff_mul(ecur, eq);  // E(x) on the row's cube points
-                                    const ff v = ff_mul(ff{hi, __fmul_rn(rem, scl)}, ecur);
-                                    hi = v.hi;
-                                    rem = v.lo;
-                                    scl = 1.0f;
+                        for (int hh = 0; hh < 2; hh++) {
+                            const int c = 2 * c2 + hh;
+                            const uint32_t mc = rmask >> (8 * c);
+                            if (__any_sync(0xffffffffu, (mc & 0xFFu) != 0u)) {
+                                uint32_t r2[8], r3[8], r4[8], r5[8];
+                                const float4 csa = reinterpret_cast<const float4 *>(sm.cs)[2 * c];
+                                const float4 csb = reinterpret_cast<const float4 *>(sm.cs)[2 * c + 1];
+                                const float csv[8] = {csa.x, csa.y, csa.z, csa.w, csb.x, csb.y, csb.z, csb.w};
+                                tc::tmem_ld8(tbase + 8 * c, r2);
+                                tc::tmem_ld8(tbase + 32 + 8 * c, r3);
+                                tc::tmem_ld8(tbase + 64 + 8 * c, r4);
+                                tc::tmem_ld8(tbase + 96 + 8 * c, r5);
+                                tc::tmem_wait_ld32(r2, r3, r4, r5);
+#pragma unroll
+                                for (int i = 0; i < 8; i++) {
+                                    const int x = 8 * c + i;
+                                    const bool in = (mc >> i) & 1u;  // straight-line code: selects, no branches
+                                    // value = scl * (D2 + D3 2^-10 + D4 2^-20 + D5 2^-30) as hi + lo with
+                                    // lo the exact remainder (fast two-sum), then an exact two-sum into
+                                    // acc_hi: acc_lo then only gathers rounding errors and remainders,
+                                    // so it stays ~2^-24 below acc_hi however many pairs a point sees
+                                    const float d2 = __uint_as_float(r2[i]);
+                                    const float corr = __fmaf_rn(__uint_as_float(r5[i]), 9.313225746154785e-10f,
+                                                       __fmaf_rn(__uint_as_float(r4[i]), 9.5367431640625e-07f,
+                                                                 __fmul_rn(__uint_as_float(r3[i]), 0.0009765625f)));
+                                    float scl = __fmul_rn(rs, csv[i]);
+                                    const float h0 = __fadd_rn(d2, corr);
+                                    float hi = __fmul_rn(h0, scl);
+                                    float rem = __fsub_rn(corr, __fsub_rn(h0, d2));  // lo = rem scl exactly
+                                    if constexpr (kGeneral) {
+                                        if (x > x0) ecur = ff_mul(ecur, eq);  // E(x) on the row's cube points
+                                        const ff v = ff_mul(ff{hi, __fmul_rn(rem, scl)}, ecur);
+                                        hi = v.hi;
+                                        rem = v.lo;
+                                        scl = 1.0f;
+                                    }
+                                    float &ah = acc_hi[8 * hh + i];
+                                    const float sv = __fadd_rn(ah, hi);
+                                    const float bb = __fsub_rn(sv, ah);
+                                    const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
+                                    if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fmaf_rn(rem, scl, err));
+                                    ah = in ? sv : ah;
                                 }
-                                const float sv = __fadd_rn(acc_hi[i], hi);
-                                const float bb = __fsub_rn(sv, acc_hi[i]);
-                                const float err = __fadd_rn(__fsub_rn(acc_hi[i], __fsub_rn(sv, bb)), __fsub_rn(hi, bb));
-                                if (in) acc_lo[x] = __fadd_rn(acc_lo[x], __fmaf_rn(rem, scl, err));
-                                acc_hi[i] = in ? sv : acc_hi[i];
                             }
                         }
-                        float t8[8];
+                        float t16[16];
 #pragma unroll
-                        for (int i = 0; i < 8; i++) t8[i] = acc_hi[i];
+                        for (int i = 0; i < 16; i++) t16[i] = acc_hi[i];
 #pragma unroll
-                        for (int i = 0; i < TX - 8; i++) acc_hi[i] = acc_hi[i + 8];
+                        for (int i = 0; i < TX - 16; i++) acc_hi[i] = acc_hi[i + 16];
 #pragma unroll
-                        for (int i = 0; i < 8; i++) acc_hi[TX - 8 + i] = t8[i];
+                        for (int i = 0; i < 16; i++) acc_hi[TX - 16 + i] = t16[i];
                     }
                 }
                 tc::fence_before_sync();
