@@ -676,9 +676,20 @@ __device__ void recentre_x(const PairBuf &pb, ff tc, ff *out, const float (*bin)
     }
 }
 
-// mask of two packed halves from bits 0 (low half) and 1 (high half) of b
-__device__ __forceinline__ uint32_t half_mask(uint32_t b) {
-    return ((0u - (b & 1u)) & 0x0000FFFFu) | ((0u - ((b >> 1) & 1u)) & 0xFFFF0000u);
+// masks of the 8 packed halves of one 16-byte chunk from bits 0..7 of b (bit k:
+// half k, all ones or zero).  One multiply per 4 bits moves bit k to the top of
+// byte k (the copies lie 7 bits apart, so no carries), and prmt, whose selector
+// nibbles with the top bit set replicate the sign of the selected byte, spreads
+// each byte's top bit over the two bytes of its half.
+__device__ __forceinline__ uint4 chunk_mask(uint32_t b) {
+    const uint32_t lo = ((b & 0xFu) * 0x10204080u) & 0x80808080u;
+    const uint32_t hi = (((b >> 4) & 0xFu) * 0x10204080u) & 0x80808080u;
+    uint4 m;
+    asm("prmt.b32 %0, %1, 0, 0x9988;" : "=r"(m.x) : "r"(lo));
+    asm("prmt.b32 %0, %1, 0, 0xBBAA;" : "=r"(m.y) : "r"(lo));
+    asm("prmt.b32 %0, %1, 0, 0x9988;" : "=r"(m.z) : "r"(hi));
+    asm("prmt.b32 %0, %1, 0, 0xBBAA;" : "=r"(m.w) : "r"(hi));
+    return m;
 }
 
 // The NSL slices of one K = 16 operand row (v[k] for k < kNPow, zero beyond),
@@ -1156,7 +1167,7 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
             double *grid = A.grids.p[td.level];
             const int64_t row = ((int64_t)(td.t[2] * TZ + z) * lv.ngrid[1] + (td.t[1] * TY + y)) * lv.ngrid[0] +
                                 td.t[0] * TX;
-            // 8 points per iteration, acc_hi rotated by 8 as in the readout (compact code)
+            // 8 points per iteration, acc_hi rotated by 8 after each (compact code)
 #pragma unroll 1
             for (int c = 0; c < TX / 8; c++) {
 #pragma unroll
@@ -1343,12 +1354,7 @@ __global__ void __launch_bounds__(NTHR, kGeneral ? 3 : 4) k_integrate_tiled(Mixe
                                                 : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
                         for (int v = 0; v < TX / 8; v++) {
-                            const uint32_t mv = M >> (8 * v);
-                            uint4 mk;
-                            mk.x = half_mask(mv);
-                            mk.y = half_mask(mv >> 2);
-                            mk.z = half_mask(mv >> 4);
-                            mk.w = half_mask(mv >> 6);
+                            const uint4 mk = chunk_mask(M >> (8 * v));
                             const int o16 = (r >> 3) * 16 + (v & 1) * 8 + (r & 7);  // umma_off / 16
 #pragma unroll
                             for (int q = 0; q < NSL; q++)
