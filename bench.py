@@ -496,7 +496,7 @@ def main():
                 "items_per_launch": items,
                 "peak_source": "bf16 sustained, MEASURED_PEAKS.json (of measured)",
                 "limiter": "FP32/integer instruction issue of the float-float stages, not the tensor pipe "
-                           "(tensor pipe active ~5%, issue slots busy 63% collocate / 53% integrate in the ncu captures)"}
+                           "(tensor pipe active ~5%, issue slots busy 62% collocate / 52% integrate in the ncu captures)"}
     else:
         hbm = peaks.get("hbm_gbs") or 6800.0
         gbytes_alg = 16.0 * points  # FP64 read+write per cube point (no reuse)
