@@ -885,7 +885,12 @@ static int stage(gpw_taskset *ts, HostStage **out) {
         e = cudaMalloc(&h.d_pab, sizeof(double) * std::max<int64_t>(ts->pab_extent, 1));
         for (int l = 0; l < ts->plan->nlevels && e == cudaSuccess; l++)
             e = cudaMalloc(&h.d_grids[l], sizeof(double) * ts->plan->lv[l].grid_elems);
-        if (e != cudaSuccess) return cuda_fail(e, "host staging");
+        if (e != cudaSuccess) {  // all or nothing: the next call allocates again
+            cudaFree(h.d_pab);
+            for (int l = 0; l < GPW_MAX_LEVELS; l++) cudaFree(h.d_grids[l]);
+            h = HostStage();
+            return cuda_fail(e, "host staging");
+        }
     }
     *out = &h;
     return GPW_SUCCESS;
@@ -953,9 +958,6 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
     }
     gd.ortho = use_ortho ? 1 : 0;
     // The reference's callers make this call once per pair, many times over the
-    // same grid: the plan (one per grid geometry) and the device buffers stay in a
-    // per-thread cache, so a call is the host set-up, three copies, two launches.
-    // The reference's callers make this call once per pair, many times over the
     // same grid: the plan (one per grid geometry), a device buffer and a pinned
     // host mirror of it stay in a per-thread cache, so a call is the host set-up,
     // one copy in (geometry, cube list, block, grid), two launches and one copy
@@ -985,9 +987,13 @@ int gpw_collocate_pgf_product_rspace(int compute_tau, int use_ortho, int la_max,
         C.release();
         int st = gpw_plan_create(&C.plan, 1, &gd, dev);
         if (st) return st;
+        const cudaError_t e = cudaMalloc(&C.d_coef, sizeof(double) * ncoef(kMaxLp));
+        if (e != cudaSuccess) {
+            C.release();  // no half-built cache for the next call to reuse
+            return cuda_fail(e, "gpw_collocate_pgf_product_rspace: coefficient buffer");
+        }
         C.device = dev;
         C.desc = gd;
-        GPW_CUDA(cudaMalloc(&C.d_coef, sizeof(double) * ncoef(kMaxLp)));
     }
     gpw_task t;
     memset(&t, 0, sizeof t);

@@ -2092,6 +2092,7 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
         cudaFree(M->d_iimg);
         M->d_items = nullptr;
         M->d_iimg = nullptr;
+        M->cap_items = 0;  // a failed allocation below leaves nothing to reuse
         const int64_t cap = std::max<int64_t>(nitems + nitems / 16, 1);
         if ((e = cudaMalloc(&M->d_items, sizeof(uint64_t) * cap)) != cudaSuccess) return fail(e);
         if ((e = cudaMalloc(&M->d_iimg, sizeof(ItemImg) * cap)) != cudaSuccess) return fail(e);
@@ -2102,6 +2103,7 @@ int mixed_rebin(TaskSet &ts, std::string &err) {
         cudaFree(M->d_start);
         M->d_tiles = nullptr;
         M->d_start = nullptr;
+        M->cap_units = 0;
         const int64_t cap = std::max<int64_t>(nunits + nunits / 16, 1);
         if ((e = cudaMalloc(&M->d_tiles, sizeof(TileDesc) * cap)) != cudaSuccess) return fail(e);
         if ((e = cudaMalloc(&M->d_start, sizeof(int64_t) * 2 * cap)) != cudaSuccess) return fail(e);
