@@ -1096,14 +1096,17 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                     // bits x0..x1 of the row: the points of this pair's sphere on the row
                     const uint32_t rmask =
                         x0 > x1 ? 0u : (uint32_t)(((2ull << x1) - 1ull) & ~((1ull << x0) - 1ull));
-                    // two chunks of 8 x per iteration (a compact loop body: instruction fetch is
-                    // a stall of this kernel); acc_hi[0..15] always holds the current chunks'
-                    // sums, rotated by 16 after each iteration (two rotations restore the order)
+                    // kCh chunks of 8 x per iteration (a compact loop body: instruction fetch
+                    // is a stall of this kernel); acc_hi[0 .. 8 kCh) always holds the current
+                    // chunks' sums, rotated by 8 kCh after each iteration (TX / (8 kCh)
+                    // rotations restore the order).  Two chunks halve the register moves of
+                    // the rotation; the general-cell body, longer by the cross factor, keeps one.
+                    constexpr int kCh = kGeneral ? 1 : 2;
 #pragma unroll 1
-                    for (int c2 = 0; c2 < TX / 16; c2++) {
+                    for (int c2 = 0; c2 < TX / (8 * kCh); c2++) {
 #pragma unroll
-                        for (int hh = 0; hh < 2; hh++) {
-                            const int c = 2 * c2 + hh;
+                        for (int hh = 0; hh < kCh; hh++) {
+                            const int c = kCh * c2 + hh;
                             const uint32_t mc = rmask >> (8 * c);
                             if (__any_sync(0xffffffffu, (mc & 0xFFu) != 0u)) {
                                 uint32_t r2[8], r3[8], r4[8], r5[8];
@@ -1147,13 +1150,13 @@ __global__ void __launch_bounds__(NTHR, 4) k_collocate_tiled(MixedArgs A) {
                                 }
                             }
                         }
-                        float t16[16];
+                        float tr[8 * kCh];
 #pragma unroll
-                        for (int i = 0; i < 16; i++) t16[i] = acc_hi[i];
+                        for (int i = 0; i < 8 * kCh; i++) tr[i] = acc_hi[i];
 #pragma unroll
-                        for (int i = 0; i < TX - 16; i++) acc_hi[i] = acc_hi[i + 16];
+                        for (int i = 0; i < TX - 8 * kCh; i++) acc_hi[i] = acc_hi[i + 8 * kCh];
 #pragma unroll
-                        for (int i = 0; i < 16; i++) acc_hi[TX - 16 + i] = t16[i];
+                        for (int i = 0; i < 8 * kCh; i++) acc_hi[TX - 8 * kCh + i] = tr[i];
                     }
                 }
                 tc::fence_before_sync();
