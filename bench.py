@@ -51,7 +51,56 @@ def parse():
     ap.add_argument("--dropin", type=int, default=0, metavar="CALLS",
                     help="instead: time CALLS calls of the single-pair drop-in entry on each of the reference's "
                          "task fixtures (host grid in and out, as the reference's replay calls it)")
+    ap.add_argument("--ref-calibration", type=int, default=0, metavar="PAIRS",
+                    help="instead: where the reference's library was built here (oracle/_ref), time one-core "
+                         "collocation of PAIRS random pairs of the workload with the CPU baseline's code and with "
+                         "the reference's own code, built as its Makefile builds it and with its asserts")
     return ap.parse_args()
+
+
+def ref_calibration(args) -> None:
+    """The CPU baseline's code (the C restatement) against the reference's own
+    grid_collocate_pgf_product_rspace on the same pairs, grids and core: how far
+    the baseline's speed stands from the reference's.  Needs the reference
+    library built from its sources (oracle/_ref), which exists only where the
+    reference tree does; prints one JSON line."""
+    from libgpw_gb300 import tasks as T
+    from oracle import oracle as O
+
+    O.build()
+    need = [os.path.join(ROOT, "oracle", "_ref", f) for f in ("libgpwref.so", "libgpwref_ndebug.so")]
+    if not all(os.path.exists(f) for f in need):
+        print(json.dumps({"metric": "CPU collocate ms per pair", "unavailable": "reference library not built here"}))
+        return
+    wl = T.config(args.config, npairs=args.npairs)
+    idx = np.random.default_rng(1).choice(wl.ntasks, size=min(args.ref_calibration, wl.ntasks), replace=False)
+    tasks = [O.task_dict(wl, int(i)) for i in idx]
+    kinds = {"restatement": False, "reference": "ndebug", "reference_with_asserts": True}
+    grids = {k: [np.zeros(T.grid_shape(g)) for g in wl.levels] for k in kinds}
+    levels = [int(wl.tasks[int(i)]["level"]) for i in idx]
+
+    def run(kind):
+        for t, lvl in zip(tasks, levels):
+            if O.collocate(t, grids[kind][lvl], use_ref=kinds[kind]):
+                raise RuntimeError(f"{kind}: collocate failed")
+
+    ms = {k: [] for k in kinds}
+    for k in kinds:  # warm-up pass (page faults of the grids)
+        run(k)
+    for _ in range(2):
+        for k in kinds:
+            t0 = time.perf_counter()
+            run(k)
+            ms[k].append((time.perf_counter() - t0) / len(tasks) * 1e3)
+    ref_grids = grids["reference"]
+    err = max(float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+              for a, b in zip(grids["restatement"], ref_grids))
+    print(json.dumps({"metric": "CPU collocate ms per pair", "config": {"workload": wl.name, "pairs": len(tasks)},
+                      "cores": 1, "ms_per_pair": {k: min(v) for k, v in ms.items()},
+                      "restatement_vs_reference_grid_rel_l2": err,
+                      "reference_build": "grid_base_ref_c.cc with -O2 -DNDEBUG, as the reference's Makefile "
+                                         "builds its library (without its x86 -mavx2 and MKL flags); "
+                                         "reference_with_asserts: the build the parity fixtures use"}))
 
 
 def dropin_bench(calls: int) -> None:
@@ -293,6 +342,9 @@ def reference_arm(args):
 # ----------------------------------------------------------------------------
 def main():
     args = parse()
+    if args.ref_calibration:
+        ref_calibration(args)
+        return
     if args.dropin:
         dropin_bench(args.dropin)
         return

@@ -356,6 +356,11 @@ static int ortho_cube(const pair_t *p, int adj, const double dh[3][3], const dou
             return GPW_ERR_INVALID_ARG;
         }
     }
+    /* grid index of every x of the cube box, once per pair (as the reference's map,
+     * grid_base_ref_c.cc:318-351): no modulo per point */
+    int *xmap = (int *)malloc(sizeof(int) * n[0]);
+    for (int g = 0; g < n[0]; g++)
+        xmap[g] = grid_index(periodic[0], cc[0], g + lo[0], lb_cube[0], lb_grid[0], npts[0], ngrid[0]);
     double cxy[NPOW][NPOW], cx[NPOW];
     int status = 0;
     for (int kg = cb->kgmin; kg <= 1 - cb->kgmin && !status; kg++) {
@@ -390,8 +395,31 @@ static int ortho_cube(const pair_t *p, int adj, const double dh[3][3], const dou
             } else {
                 memset(cx, 0, sizeof(cx));
             }
-            for (int ig = igmin; ig <= 1 - igmin; ig++) {
-                int i = grid_index(periodic[0], cc[0], ig, lb_cube[0], lb_grid[0], npts[0], ngrid[0]);
+            int ig = igmin;
+            if (!adj) {
+                /* four points at a time: four independent sums, each in the order of the
+                 * one-point loop below (the same result); groups with a point outside the
+                 * window are left to that loop */
+                for (; ig + 3 <= 1 - igmin; ig += 4) {
+                    const int *im = xmap + (ig - lo[0]);
+                    if (im[0] < 0 || im[1] < 0 || im[2] < 0 || im[3] < 0) break;
+                    const double *X = tab[0] + (ig - lo[0]) * (lp + 1);
+                    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                    for (int lx = 0; lx <= lp; lx++) {
+                        s0 += cx[lx] * X[lx];
+                        s1 += cx[lx] * X[(lp + 1) + lx];
+                        s2 += cx[lx] * X[2 * (lp + 1) + lx];
+                        s3 += cx[lx] * X[3 * (lp + 1) + lx];
+                    }
+                    const int64_t row = ((int64_t)k * ngrid[1] + j) * ngrid[0];
+                    grid[row + im[0]] += s0;
+                    grid[row + im[1]] += s1;
+                    grid[row + im[2]] += s2;
+                    grid[row + im[3]] += s3;
+                }
+            }
+            for (; ig <= 1 - igmin; ig++) {
+                int i = xmap[ig - lo[0]];
                 if (i < 0) { status = GPW_ERR_OUT_OF_WINDOW; break; }
                 const double *X = tab[0] + (ig - lo[0]) * (lp + 1);
                 int64_t gidx = ((int64_t)k * ngrid[1] + j) * ngrid[0] + i;
@@ -414,6 +442,7 @@ static int ortho_cube(const pair_t *p, int adj, const double dh[3][3], const dou
                     for (int lz = 0; lz <= lp - ly - lx; lz++)
                         w[(lz * NPOW + ly) * NPOW + lx] += cxy[ly][lx] * Z[lz];
     }
+    free(xmap);
     for (int d = 0; d < 3; d++) free(tab[d]);
     return status;
 }

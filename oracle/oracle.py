@@ -19,6 +19,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 _lib = None
 _ref = None
+_ref_ndebug = None
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
@@ -62,14 +63,19 @@ def ref_available() -> bool:
     return os.path.exists(os.path.join(HERE, "_ref", "libgpwref.so"))
 
 
-def ref():
-    global _ref
-    if _ref is None:
-        L = C.CDLL(os.path.join(HERE, "_ref", "libgpwref.so"))
+def ref(ndebug: bool = False):
+    """The reference's own collocate: built with its asserts (parity), or with
+    -DNDEBUG as the reference's Makefile builds its library (timing)."""
+    global _ref, _ref_ndebug
+    if (_ref_ndebug if ndebug else _ref) is None:
+        L = C.CDLL(os.path.join(HERE, "_ref", "libgpwref_ndebug.so" if ndebug else "libgpwref.so"))
         L.gpwref_collocate.argtypes = _ARGS
         L.gpwref_collocate.restype = C.c_int
-        _ref = L
-    return _ref
+        if ndebug:
+            _ref_ndebug = L
+        else:
+            _ref = L
+    return _ref_ndebug if ndebug else _ref
 
 
 def _i3(x):
@@ -91,10 +97,11 @@ def _args(t: dict, pab_or_v, out):
             np.ascontiguousarray(pab_or_v, dtype=np.float64).reshape(-1), out)
 
 
-def collocate(t: dict, grid: np.ndarray, use_ref: bool = False) -> int:
-    """grid += rho of one task (dict in the task-v1 vocabulary)."""
+def collocate(t: dict, grid: np.ndarray, use_ref: bool | str = False) -> int:
+    """grid += rho of one task (dict in the task-v1 vocabulary): the restatement,
+    the reference (use_ref=True) or its -DNDEBUG build (use_ref="ndebug")."""
     assert grid.dtype == np.float64 and grid.flags.c_contiguous
-    f = ref().gpwref_collocate if use_ref else lib().gpwo_collocate
+    f = ref(ndebug=use_ref == "ndebug").gpwref_collocate if use_ref else lib().gpwo_collocate
     return f(*_args(t, t["pab"], grid.reshape(-1)))
 
 
