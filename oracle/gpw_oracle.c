@@ -783,6 +783,32 @@ static void *job_run(void *arg) {
     return NULL;
 }
 
+/* The threads' private grids (or hab arrays) summed into thread 0's, each
+ * element over t = 1, 2, ... in order (the result of a serial sum); nparts
+ * threads take contiguous parts of the arrays. */
+typedef struct {
+    job_t *jobs;
+    int nthreads, adj, nlevels, part, nparts;
+    const gpw_grid_desc *levels;
+    double *const *grids;
+    double *hab;
+    int64_t hab_len;
+} reduce_t;
+
+static void *reduce_run(void *arg) {
+    const reduce_t *R = (const reduce_t *)arg;
+    for (int l = 0; l < (R->adj ? 1 : R->nlevels); l++) {
+        const int64_t n = R->adj ? R->hab_len : level_size(&R->levels[l]);
+        const int64_t i0 = n * R->part / R->nparts, i1 = n * (R->part + 1) / R->nparts;
+        double *out = R->adj ? R->hab : R->grids[l];
+        for (int t = 1; t < R->nthreads; t++) {
+            const double *src = R->adj ? R->jobs[t].hab : R->jobs[t].grids[l];
+            for (int64_t i = i0; i < i1; i++) out[i] += src[i];
+        }
+    }
+    return NULL;
+}
+
 /* grids[l] += rho (adj 0) or hab += <V|basis> (adj 1) for a task batch. */
 int gpwo_batch(int adj, int compute_tau, const gpw_task *tasks, int64_t ntasks,
                const gpw_grid_desc *levels, int nlevels, const int *sphere_table,
@@ -808,20 +834,26 @@ int gpwo_batch(int adj, int compute_tau, const gpw_task *tasks, int64_t ntasks,
     for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, job_run, &jobs[t]);
     job_run(&jobs[0]);
     for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+    if (nthreads > 1) {
+        reduce_t *R = (reduce_t *)calloc((size_t)nthreads, sizeof(reduce_t));
+        for (int t = 0; t < nthreads; t++) {
+            R[t].jobs = jobs; R[t].nthreads = nthreads; R[t].adj = adj; R[t].nlevels = nlevels;
+            R[t].part = t; R[t].nparts = nthreads; R[t].levels = levels; R[t].grids = grids;
+            R[t].hab = hab; R[t].hab_len = hab_len;
+        }
+        for (int t = 1; t < nthreads; t++) pthread_create(&th[t], NULL, reduce_run, &R[t]);
+        reduce_run(&R[0]);
+        for (int t = 1; t < nthreads; t++) pthread_join(th[t], NULL);
+        free(R);
+    }
     for (int t = 0; t < nthreads; t++) {
         job_t *J = &jobs[t];
         if (J->status && !status) status = J->status;
         if (t > 0) {
-            if (!adj) {
-                for (int l = 0; l < nlevels; l++) {
-                    int64_t n = level_size(&levels[l]);
-                    for (int64_t i = 0; i < n; i++) grids[l][i] += J->grids[l][i];
-                    free(J->grids[l]);
-                }
-            } else {
-                for (int64_t i = 0; i < hab_len; i++) hab[i] += J->hab[i];
+            if (!adj)
+                for (int l = 0; l < nlevels; l++) free(J->grids[l]);
+            else
                 free(J->hab);
-            }
         }
         free(J->grids);
     }
