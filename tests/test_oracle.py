@@ -100,6 +100,29 @@ def test_reference_direct(oracle_lib):
         assert rel_l2(b, a) <= 1e-13
 
 
+@pytest.mark.parametrize("cfg,npairs,tol", [(1, 16, 1e-13), (2, 24, 1e-13), (3, 12, 1e-11), (5, 24, 1e-13)])
+def test_reference_on_benchmark_workloads(oracle_lib, cfg, npairs, tol):
+    """The restatement against the reference's own collocate, pair by pair, on
+    random pairs of the benchmark workloads (their own exponent, radius, l and
+    cell distributions: multigrid levels, the general cell's wrapping cubes, the
+    256^3 grid), and the reference's -DNDEBUG build (the one bench.py
+    --ref-calibration times) against its parity build.  General cells: the
+    reference's row recurrence drifts up to ~2e-12 from exact exponentials."""
+    if not oracle_lib.ref_available():
+        pytest.skip("reference library not built on this machine")
+    wl = T.config(cfg, npairs=2000 if cfg in (2, 5) else None, seed=31 + cfg)
+    rng = np.random.default_rng(cfg)
+    for i in rng.choice(wl.ntasks, size=npairs, replace=False):
+        d = oracle_lib.task_dict(wl, int(i))
+        lvl = wl.levels[int(wl.tasks[int(i)]["level"])]
+        ref, nd, port = (np.zeros(T.grid_shape(lvl)) for _ in range(3))
+        assert oracle_lib.collocate(d, ref, use_ref=True) == 0
+        assert oracle_lib.collocate(d, nd, use_ref="ndebug") == 0
+        assert oracle_lib.collocate(d, port) == 0
+        assert np.array_equal(nd, ref)
+        assert rel_l2(port, ref) <= tol
+
+
 @pytest.mark.parametrize("name", TASK_NAMES)
 def test_task_file_writer_round_trip(oracle_lib, name, tmp_path):
     """write_task_file writes the reference's task lines with every nonzero grid
