@@ -156,7 +156,9 @@ int64_t gpw_taskset_pab_extent(const gpw_taskset *ts);
  * grid[level] += sum over tasks of the pair density (grid_base_ref_c.cc:1018).
  * d_pab and d_grids[l] are device pointers; asynchronous on `stream`
  * (a cudaStream_t, NULL = legacy default); no allocation, so the call can be
- * captured in a CUDA graph.
+ * captured in a CUDA graph.  A task set's work buffers (coefficients, moments,
+ * work queues) serve one call at a time: calls on one task set that could
+ * overlap on the GPU belong on one stream; different task sets are independent.
  */
 int gpw_collocate(gpw_taskset *ts, int precision, const double *d_pab,
                   double *const *d_grids, void *stream);
@@ -285,7 +287,11 @@ int gpw_collocate_noalloc(const gpw_grid_desc *level, const gpw_task *tasks,
                           int ntasks, int compute_tau, const double *d_pab,
                           double *d_grid, void *stream);
 
-/* Host-buffer convenience calls (copies inside, synchronous) ------------- */
+/* Host-buffer convenience calls (copies inside, synchronous) -------------
+ * The same accumulation as gpw_collocate / gpw_integrate from host arrays
+ * (pinned or pageable).  Device staging buffers are allocated on a task set's
+ * first host-buffer call and kept until gpw_taskset_destroy; calls on one task
+ * set from several host threads must be serialised by the caller. */
 int gpw_collocate_host(gpw_taskset *ts, int precision, const double *h_pab,
                        double *const *h_grids);
 int gpw_integrate_host(gpw_taskset *ts, int precision, double *const *h_grids,
