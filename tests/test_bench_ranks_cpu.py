@@ -87,3 +87,25 @@ def test_reference_arm_line(monkeypatch, oracle_lib):
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
     assert d["config"]["workload"] and d["metric"] == bench.METRIC
+
+
+def test_ref_calibration_line():
+    """bench.py --ref-calibration: the CPU baseline's code against the reference's
+    own collocate on the same pairs (where the reference library was built)."""
+    import json
+
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import oracle as O
+
+    if not O.ref_available():
+        pytest.skip("reference library not built on this machine")
+    args = types.SimpleNamespace(ref_calibration=12, config=1, npairs=None)
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        bench.ref_calibration(args)
+    line = json.loads(buf.getvalue().strip().splitlines()[-1])
+    assert set(line["ms_per_pair"]) == {"restatement", "reference", "reference_with_asserts"}
+    assert all(v > 0 for v in line["ms_per_pair"].values())
+    assert line["restatement_vs_reference_grid_rel_l2"] <= 1e-13
+    assert line["config"]["pairs"] == 12
