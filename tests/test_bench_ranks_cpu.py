@@ -1,6 +1,7 @@
-"""The multi-rank parts of bench.py on CPU: two gloo ranks (one process each, as
-torchrun launches them) take the maximum of their per-rank times, and the
-reference arm prints its line from rank 0 only."""
+"""The CPU parts of bench.py: two gloo ranks (one process each, as torchrun
+launches them) take the maximum of their per-rank times, the reference arm
+prints its line from rank 0 only, and --ref-calibration compares the CPU
+baseline's code with the reference's own."""
 import contextlib
 import io
 import os
